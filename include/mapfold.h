@@ -1,0 +1,218 @@
+/*
+ * mapfold.h -- C ABI of the GB300 map-folding counting engine.
+ *
+ * The reference (johnowhitaker/map_folding) exposes its two counting paths
+ * only as process CLIs, plus one in-process C ABI (the WASM kernel's
+ * solve_cases).  Each entry point below names the reference interface it
+ * stands in for.  Conventions:
+ *   - every function returns an mf_status (0 = MF_OK); mf_last_error()
+ *     gives a one-line reason for the last failure on the calling thread;
+ *   - pointers named d_* are device pointers on the current CUDA device;
+ *     everything else is host memory;
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default);
+ *   - counts are exact unsigned integers: uint64 per state / per case, and
+ *     128-bit totals as two uint64 words {lo, hi}.
+ *
+ * No function here takes or returns any framework type.
+ */
+#ifndef MAPFOLD_H
+#define MAPFOLD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MF_ABI_VERSION 1
+#define MF_MAX_LEAVES 64   /* leaves (Lunnon) or cells (sym) per map */
+#define MF_MAX_DIMS 8
+#define MF_SYM_CYCLE_BYTES 64 /* one sym case: successor cell of each cell */
+
+typedef enum {
+    MF_OK = 0,
+    MF_ERR_ARG = 1,       /* bad argument: the reference's rc 1 / status 1 */
+    MF_ERR_RANGE = 2,     /* bad index range: the WASM kernel's status 2 */
+    MF_ERR_CUDA = 3,      /* a CUDA runtime call failed */
+    MF_ERR_NO_DEVICE = 4, /* no CUDA device visible */
+    MF_ERR_CAPACITY = 5,  /* caller buffer or workspace too small */
+    MF_ERR_TIMEOUT = 6    /* a bounded device-side wait ran out */
+} mf_status;
+
+/* One-line description of the last error on this thread ("" if none). */
+const char *mf_last_error(void);
+int32_t mf_abi_version(void);
+
+/* Timings and work counters of one engine call (all optional outputs). */
+typedef struct {
+    double setup_s;       /* host-side tables, prefix or case generation */
+    double h2d_s;         /* host->device copies */
+    double kernel_s;      /* device time of the counting kernels (events) */
+    double d2h_s;         /* device->host copies */
+    double total_s;       /* wall time of the whole call */
+    uint64_t units;       /* prefix states or cases counted */
+    uint64_t nodes;       /* reference nodes visited (see each entry) */
+    uint64_t tasks;       /* work items run, including device-side splits */
+    uint64_t splits;      /* work items created by device-side splitting */
+    uint64_t h2d_bytes;
+    uint64_t d2h_bytes;
+} mf_run_stats;
+
+/* Launch shape and scheduling knobs of the persistent (batched) kernels.
+ * Zero in any field selects the built-in default. */
+typedef struct {
+    uint32_t block_threads;  /* threads per CTA (multiple of 32) */
+    uint32_t blocks_per_sm;  /* resident CTAs per SM for the persistent grid */
+    uint32_t node_budget;    /* DFS nodes a thread runs between split checks */
+    uint32_t hungry_factor;  /* split while queued work < factor x threads */
+    uint64_t queue_capacity; /* device work-item slots for split subtrees */
+    uint32_t wait_limit;     /* bound on each device-side spin wait */
+    uint32_t reserved;
+} mf_batch_config;
+
+/* ======================================================================
+ * Lunnon backtracking DFS over leaves (any dimension count, <= 64 leaves)
+ * ====================================================================== */
+
+typedef struct mf_lunnon_plan mf_lunnon_plan;
+
+/* Builds the coordinate and neighbour tables for a p1 x p2 x ... map and
+ * uploads them to the current device.
+ * Replaces: mf.c:29-75 (c/d tables), gpu_folding.cu:227-264 (host tables +
+ * cudaMemcpyToSymbol), gpu_folding_v2.cu:131-163 (make_problem). */
+int32_t mf_lunnon_plan_create(const int32_t *dims, int32_t ndim, mf_lunnon_plan **out);
+void mf_lunnon_plan_destroy(mf_lunnon_plan *plan);
+/* Number of leaves n = p1*p2*...  */
+int32_t mf_lunnon_leaves(const mf_lunnon_plan *plan);
+/* Bytes per packed prefix-state record: b[0..n] as uint8, zero padded to a
+ * multiple of 16 so that each record loads as whole 16-byte vectors. */
+uint32_t mf_lunnon_state_stride(const mf_lunnon_plan *plan);
+
+/* Host prefix generation: every state at leaf depth `depth` that passes the
+ * normal-form filter, in the reference's emission order.  Writes up to `cap`
+ * records; *count_out gets the total (which may exceed cap).
+ * Replaces: gpu_folding.cu:21-121 (collect_partial_states),
+ * gpu_folding_v2.cu:220-256 (collect_states), mf_fast.cpp:223-259
+ * (count_states, with states == NULL). */
+int32_t mf_lunnon_collect(const mf_lunnon_plan *plan, int32_t depth, uint8_t *states,
+                          uint64_t cap, uint64_t *count_out);
+
+/* Plain GPU DFS, one thread per prefix state, resumed at leaf start_leaf
+ * (= depth + 1) and stopped when the search returns to it.  d_per_state
+ * (optional) receives each state's count; *d_total (optional) is ADDED to;
+ * *d_nodes (optional) is added the number of leaf insertions the reference
+ * loop would make (mf.c:136-142).
+ * Replaces: gpu_folding.cu:123-207 (compute_counts) and its launch
+ * :287-299; gpu_folding_v2.cu:381-453 (solve_kernel). */
+int32_t mf_lunnon_count_states(const mf_lunnon_plan *plan, int32_t start_leaf,
+                               const uint8_t *d_states, uint64_t num_states,
+                               uint64_t *d_per_state, uint64_t *d_total, uint64_t *d_nodes,
+                               void *stream);
+
+/* Whole-map count: prefix generation to `depth`, host->device copy, plain
+ * (mode 0) or batched work-stealing (mode 1) kernel, device->host copy.
+ * *count_out is the folding count.  This is what `gpu_folding <n> <depth>`
+ * computes (gpu_folding.cu:209-311).  depth < 0 picks a default. */
+int32_t mf_lunnon_count(const mf_lunnon_plan *plan, int32_t depth, int32_t mode,
+                        const mf_batch_config *cfg, uint64_t *count_out,
+                        uint64_t *states_out, mf_run_stats *stats);
+
+/* Batched uneven launch: all prefix states of `num_plans` maps (each at its
+ * own depth) in ONE persistent work-stealing kernel that splits subtrees on
+ * the device.  counts_out[k] receives map k's folding count; depths may be
+ * NULL and a negative depth picks a default.
+ * No reference counterpart in one call: the reference runs one map per
+ * process (gpu_folding_v2.cu:476-542 batches states of a single map). */
+int32_t mf_lunnon_batch_count(const mf_lunnon_plan *const *plans, int32_t num_plans,
+                              const int32_t *depths, const mf_batch_config *cfg,
+                              uint64_t *counts_out, mf_run_stats *stats);
+
+/* ======================================================================
+ * sym_fold: symmetry-reduced square counting (n <= 8)
+ * ====================================================================== */
+
+/* The four edge pages of an n x n grid in centre-out spiral numbering:
+ * out[page*64 + cell] = neighbour across that page's edge, or n*n.
+ * Replaces: sym_fold.cpp:122-173 (build_map, make_edges). */
+int32_t mf_sym_edges(int32_t n, uint8_t *out);
+
+typedef struct mf_sym_plan mf_sym_plan;
+
+/* Centre enumeration, D4 x stack-reversal dedup and the expansion index for
+ * cases at `expanded_n` cells (0 = the reference default: 24 for n >= 7;
+ * n = 6 always uses its 16-cell centre).  n must be 6..8.
+ * Replaces: sym_fold.cpp:252-265, 316-408, 703-745. */
+int32_t mf_sym_plan_create(int32_t n, int32_t expanded_n, mf_sym_plan **out);
+void mf_sym_plan_destroy(mf_sym_plan *plan);
+/* Representatives before expansion and their orbit sizes. */
+int32_t mf_sym_plan_info(const mf_sym_plan *plan, int32_t *n, int32_t *start_i,
+                         uint64_t *center_cases, uint64_t *reduced_cases,
+                         uint64_t *total_cases);
+
+/* Cases [start_case, start_case + max_cases) of the deterministic emission
+ * order (max_cases == 0: to the end), each as a 64-byte cycle plus its orbit
+ * multiplier.  Seeks through a per-representative case-count index instead
+ * of walking every earlier case.  *count_out gets the number selected.
+ * Replaces: sym_fold.cpp:491-527 (recurse_stream_cases), :731-745. */
+int32_t mf_sym_cases(const mf_sym_plan *plan, uint64_t start_case, uint64_t max_cases,
+                     uint8_t *cycles, uint64_t *mults, uint64_t cap, uint64_t *count_out);
+
+/* Plain GPU count, one thread per case: d_counts[k] = completions of case k
+ * from cell start_i up to (excluding) stop_i, i.e. the number of distinct
+ * cycles reaching stop_i cells (stop_i = n*n: complete foldings).  *d_nodes
+ * (optional) is added the number of recurse_count calls (sym_fold.cpp:219).
+ * Replaces: sym_fold.cpp:219-233 (recurse_count) run per case by
+ * solve_cases_parallel :410-489. */
+int32_t mf_sym_count_cases(int32_t n, int32_t start_i, int32_t stop_i,
+                           const uint8_t *d_cycles, uint64_t num_cases,
+                           uint64_t *d_counts, uint64_t *d_nodes, void *stream);
+
+/* Device workspace the batched sym kernel needs for `cfg`. */
+uint64_t mf_sym_workspace_bytes(const mf_batch_config *cfg);
+
+/* Batched GPU count: one persistent work-stealing kernel over all cases,
+ * splitting heavy subtrees on the device.  Same outputs as
+ * mf_sym_count_cases.  d_workspace must hold mf_sym_workspace_bytes(cfg)
+ * bytes; *d_status (optional, device uint32[4]) receives {error flag,
+ * tasks run, splits, 0}.
+ * Replaces: the same reference lines as mf_sym_count_cases; the reference
+ * balances only across host threads (sym_fold.cpp:456-488). */
+int32_t mf_sym_count_cases_batched(int32_t n, int32_t start_i, int32_t stop_i,
+                                   const uint8_t *d_cycles, uint64_t num_cases,
+                                   uint64_t *d_counts, uint64_t *d_nodes,
+                                   void *d_workspace, uint64_t workspace_bytes,
+                                   const mf_batch_config *cfg, void *stream);
+
+/* Count cases [start_case, start_case + max_cases) of a plan (max_cases 0:
+ * to the end): answer = n*n * sum(multiplier * count), the number
+ * `sym_fold` prints for that chunk.  mode 0 = plain kernel, 1 = batched.
+ * Replaces: sym_fold.cpp:410-489 / 529-620 and :764. */
+int32_t mf_sym_plan_solve(const mf_sym_plan *plan, uint64_t max_cases, uint64_t start_case,
+                          int32_t mode, const mf_batch_config *cfg, uint64_t *answer_lo_hi,
+                          mf_run_stats *stats);
+
+/* The whole `sym_fold n threads max_cases start_case` computation with the
+ * MF_EXPANDED_N semantics: answer = n*n * sum(multiplier * count) over the
+ * selected cases (n <= 5: 2*n*n*count).  mode 0 = plain kernel, 1 =
+ * batched.  Replaces: sym_fold.cpp:649-774 (main). */
+int32_t mf_sym_solve(int32_t n, uint64_t max_cases, uint64_t start_case, int32_t expanded_n,
+                     int32_t mode, const mf_batch_config *cfg, uint64_t *answer_lo_hi,
+                     mf_run_stats *stats);
+
+/* In-process case solver with the WASM kernel's contract: case_buffer holds
+ * case_count records of 112 bytes (cycle bytes [0, n*n), uint64 LE
+ * multiplier at offset 100); output_words[8] receives the 128-bit sum of
+ * multiplier*count (LE words 0-3), the uint64 node count (words 4-5,
+ * recurse_count calls including the stop level) and the status (word 6).
+ * Status 1: n outside 2..8 or case_count > 256; status 2: start_i > stop_i
+ * or stop_i > n*n.  Counting is on the GPU.
+ * Replaces: mfah/wasm/sym_kernel.c:251-276 (solve_cases). */
+uint32_t mf_solve_cases(uint32_t n, uint32_t start_i, uint32_t stop_i,
+                        const uint8_t *case_buffer, uint32_t case_count,
+                        uint32_t *output_words);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MAPFOLD_H */

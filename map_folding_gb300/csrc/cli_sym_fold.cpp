@@ -1,0 +1,171 @@
+// cli_sym_fold.cpp -- drop-in for the reference's `sym_fold` binary.
+//
+//   sym_fold n [threads] [max_cases] [start_case]
+//
+// Same argument checks, exit codes, stdout (one decimal line) and stderr
+// key=value lines as sym_fold.cpp:622-774, including MF_STREAM_CASES,
+// MF_EXPANDED_N and MF_SETUP_ONLY.  The counting runs on the GPU; `threads`
+// is accepted and echoed.  MF_GPU_MODE=plain selects the one-thread-per-case
+// kernel instead of the batched work-stealing one.
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
+
+#include "mapfold.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+double since(Clock::time_point t) {
+    return std::chrono::duration<double>(Clock::now() - t).count();
+}
+
+std::string decimal(uint64_t lo, uint64_t hi) {
+    unsigned __int128 v = (static_cast<unsigned __int128>(hi) << 64) | lo;
+    if (v == 0) return "0";
+    std::string s;
+    while (v) {
+        s.insert(s.begin(), char('0' + int(v % 10)));
+        v /= 10;
+    }
+    return s;
+}
+
+bool parse_long(const char *text, long &out) {
+    char *end = nullptr;
+    out = std::strtol(text, &end, 10);
+    return *text != '\0' && *end == '\0';
+}
+
+bool parse_size(const char *text, unsigned long long &out) {
+    char *end = nullptr;
+    out = std::strtoull(text, &end, 10);
+    return *text != '\0' && *end == '\0';
+}
+
+void usage(const char *exe) {
+    std::fprintf(stderr, "Usage: %s n [threads] [max_cases] [start_case]\nExample: %s 6 12\n", exe,
+                 exe);
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    if (argc < 2 || argc > 5) {
+        usage(argv[0]);
+        return 1;
+    }
+    long n = 0;
+    if (!parse_long(argv[1], n)) {
+        std::fprintf(stderr, "Invalid n: %s\n", argv[1]);
+        return 2;
+    }
+    if (n < 1 || n > 8) {
+        std::fprintf(stderr, "n must be between 1 and 8\n");
+        return 1;
+    }
+    unsigned hw = std::thread::hardware_concurrency();
+    long threads = hw == 0 ? 1 : long(hw);
+    if (argc >= 3 && !parse_long(argv[2], threads)) {
+        std::fprintf(stderr, "Invalid threads: %s\n", argv[2]);
+        return 2;
+    }
+    if (threads < 1) {
+        std::fprintf(stderr, "threads must be positive\n");
+        return 1;
+    }
+    unsigned long long max_cases = 0, start_case = 0;
+    if (argc >= 4 && !parse_size(argv[3], max_cases)) {
+        std::fprintf(stderr, "Invalid max_cases: %s\n", argv[3]);
+        return 2;
+    }
+    if (argc >= 5 && !parse_size(argv[4], start_case)) {
+        std::fprintf(stderr, "Invalid start_case: %s\n", argv[4]);
+        return 2;
+    }
+    const auto t0 = Clock::now();
+    if (n <= 1) {
+        std::printf("1\n");
+        return 0;
+    }
+    if (n == 2) {
+        std::printf("8\n");
+        return 0;
+    }
+    const char *mode_env = std::getenv("MF_GPU_MODE");
+    const int mode = (mode_env && std::strcmp(mode_env, "plain") == 0) ? 0 : 1;
+    const bool stream = std::getenv("MF_STREAM_CASES") != nullptr;
+    int expanded_n = 24;
+    if (const char *e = std::getenv("MF_EXPANDED_N")) expanded_n = std::atoi(e);
+
+    uint64_t answer[2] = {0, 0};
+    mf_run_stats st{};
+    if (n <= 5) {
+        if (mf_sym_solve(int32_t(n), 0, 0, 0, mode, nullptr, answer, &st) != MF_OK) {
+            std::fprintf(stderr, "error: %s\n", mf_last_error());
+            return 2;
+        }
+        // answer = 2 n^2 raw
+        unsigned __int128 a = (static_cast<unsigned __int128>(answer[1]) << 64) | answer[0];
+        unsigned __int128 raw = a / (2 * n * n);
+        std::fprintf(stderr, "raw_count=%s\n", decimal(uint64_t(raw), uint64_t(raw >> 64)).c_str());
+    } else {
+        const int c2 = (n % 2 == 0) ? 16 : 9;
+        if (n >= 7 && (expanded_n < c2 || expanded_n > n * n)) {
+            std::fprintf(stderr, "MF_EXPANDED_N must be between %d and %ld\n", c2, n * n);
+            return 1;
+        }
+        mf_sym_plan *plan = nullptr;
+        if (mf_sym_plan_create(int32_t(n), n >= 7 ? expanded_n : 0, &plan) != MF_OK) {
+            std::fprintf(stderr, "error: %s\n", mf_last_error());
+            return 2;
+        }
+        int32_t start_i = 0;
+        uint64_t centers = 0, reduced = 0, total = 0;
+        mf_sym_plan_info(plan, nullptr, &start_i, &centers, &reduced, &total);
+        std::fprintf(stderr, "center_cases=%llu\n", (unsigned long long)centers);
+        std::fprintf(stderr, "reduced_cases=%llu\n", (unsigned long long)reduced);
+        if (n >= 7) {
+            if (stream)
+                std::fprintf(stderr, "stream_seed_cases=%llu stream_from=%d stream_to=%d\n",
+                             (unsigned long long)reduced, c2, expanded_n);
+            else
+                std::fprintf(stderr, "expanded_cases=%llu\n", (unsigned long long)total);
+        }
+        if (std::getenv("MF_SETUP_ONLY") != nullptr) {
+            // The reference prints the number of cases it holds: the centre
+            // representatives in stream mode, the expanded cases otherwise.
+            const uint64_t held = (n >= 7 && !stream) ? total : reduced;
+            std::printf("%llu\n", (unsigned long long)held);
+            std::fprintf(stderr, "n=%ld threads=%ld max_cases=%llu start_case=%llu setup_only=1 total_s=%g\n",
+                         n, threads, max_cases, start_case, since(t0));
+            mf_sym_plan_destroy(plan);
+            return 0;
+        }
+        const int rc = mf_sym_plan_solve(plan, max_cases, start_case, mode, nullptr, answer, &st);
+        mf_sym_plan_destroy(plan);
+        if (rc != MF_OK) {
+            std::fprintf(stderr, "error: %s\n", mf_last_error());
+            return 2;
+        }
+        const double el = since(t0);
+        if (stream)
+            std::fprintf(stderr, "stream selected=%llu completed=%llu producer_done=1 rate=%g/s elapsed_s=%g\n",
+                         (unsigned long long)st.units, (unsigned long long)st.units,
+                         el > 0 ? st.units / el : 0.0, el);
+        else
+            std::fprintf(stderr, "progress=%llu/%llu rate=%g/s elapsed_s=%g\n",
+                         (unsigned long long)st.units, (unsigned long long)st.units,
+                         el > 0 ? st.units / el : 0.0, el);
+    }
+    std::printf("%s\n", decimal(answer[0], answer[1]).c_str());
+    std::fprintf(stderr, "n=%ld threads=%ld max_cases=%llu start_case=%llu total_s=%g\n", n, threads,
+                 max_cases, start_case, since(t0));
+    std::fprintf(stderr, "gpu_mode=%s kernel_s=%g nodes=%llu splits=%llu\n", mode ? "batched" : "plain",
+                 st.kernel_s, (unsigned long long)st.nodes, (unsigned long long)st.splits);
+    return 0;
+}

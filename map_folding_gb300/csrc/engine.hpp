@@ -1,0 +1,164 @@
+// engine.hpp -- internal declarations shared by the host code, the kernels
+// and the C ABI of the map-folding engine.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/mapfold.h"
+
+namespace mf {
+
+// ---------------------------------------------------------------- errors --
+void set_error(const char *fmt, ...);
+void clear_error();
+const char *last_error();
+
+#define MF_TRY_CUDA(call)                                                          \
+    do {                                                                           \
+        cudaError_t mf_err_ = (call);                                              \
+        if (mf_err_ != cudaSuccess) {                                              \
+            ::mf::set_error("%s failed: %s", #call, cudaGetErrorString(mf_err_));   \
+            return MF_ERR_CUDA;                                                    \
+        }                                                                          \
+    } while (0)
+
+double now_seconds();
+
+// ------------------------------------------------------------- Lunnon ----
+// Coordinate/neighbour tables of one p1 x p2 x ... map (mf.c:29-75).
+struct LunnonTables {
+    int n = 0;
+    int dim = 0;
+    int p[MF_MAX_DIMS] = {};
+    int stride[MF_MAX_DIMS + 1] = {};
+    // next[(i*(n+1) + l)*(n+1) + m]: leaf reached from m in dimension i when
+    // leaves 1..l are placed; entry m = 0 is 0.
+    std::vector<uint8_t> next;
+    uint8_t at(int i, int l, int m) const { return next[(size_t(i) * (n + 1) + l) * (n + 1) + m]; }
+};
+
+bool build_lunnon_tables(const int32_t *dims, int ndim, LunnonTables &t, std::string &why);
+
+// Bytes per packed prefix-state record (b[0..n], padded to 16).
+inline uint32_t lunnon_state_stride(int n) { return uint32_t((n + 1 + 15) / 16 * 16); }
+
+// Prefix states at leaf depth `depth` in the reference's emission order.
+// Writes up to cap records of `stride` bytes; returns the total count.
+uint64_t collect_lunnon_states(const LunnonTables &t, int depth, uint8_t *out, uint64_t cap,
+                               uint32_t stride);
+
+// A sensible default split depth for a map with n leaves.
+int default_lunnon_depth(const LunnonTables &t);
+
+// --------------------------------------------------------------- sym -----
+constexpr int kSymCells = 64;
+
+void sym_edges(int n, uint8_t *out /* 4*64 */);
+uint64_t sym_good_host(const uint8_t *cycle, int i, const uint8_t *edges);
+
+struct SymPlan {
+    int n = 0;
+    int c = 0;            // centre side (3 odd, 4 even)
+    int seed_i = 0;       // c*c
+    int start_i = 0;      // cells placed in every case (= expanded_n)
+    uint64_t center_cases = 0;
+    std::vector<uint8_t> edges;      // 4*64
+    std::vector<uint8_t> reps;       // representatives, 64 bytes each
+    std::vector<uint64_t> rep_mult;  // orbit sizes
+    // Expansion index: the cases are the depth-start_i descendants of the
+    // representatives, emitted in DFS order.  When mid_i > seed_i the index
+    // holds every depth-mid_i prefix with the number of cases below it, so
+    // a chunk start is found by binary search instead of a walk.
+    int mid_i = 0;
+    std::vector<uint8_t> mid_cycles;
+    std::vector<uint64_t> mid_mult;
+    std::vector<uint64_t> mid_first;  // prefix sums: first case index of each
+    uint64_t total_cases = 0;
+};
+
+// Builds reps/multipliers and (host side) the expansion index at mid level
+// `mid_i` (0 = none).  mid counts are filled by `count_below` when the
+// index is used; see sym_plan_index().
+int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why);
+
+// Enumerate depth-`stop` descendants of `cycle` (cells < from placed) in DFS
+// order, calling emit(cycle) for each; emit returns false to stop early.
+// Returns false if stopped.
+template <class F>
+bool sym_expand(uint8_t *cycle, int from, int stop, const uint8_t *edges, F &&emit);
+
+// Select cases [start, start+max) into cycles/mults; returns count selected.
+uint64_t sym_select_cases(const SymPlan &plan, uint64_t start, uint64_t max_cases,
+                          uint8_t *cycles, uint64_t *mults, uint64_t cap);
+
+// -------------------------------------------------------- device side ----
+struct BatchKnobs {
+    int block_threads;
+    int blocks_per_sm;
+    uint32_t node_budget;
+    uint32_t hungry_factor;
+    uint64_t queue_capacity;
+    uint32_t wait_limit;
+};
+BatchKnobs resolve_knobs(const mf_batch_config *cfg);
+
+// Work item written by device-side splitting (96 bytes).
+struct alignas(16) TaskRecord {
+    uint32_t words[17];  // successor list of the placed items (byte per item)
+    uint32_t owner;      // result slot
+    uint64_t mask;       // remaining choices at `level`
+    uint32_t level;
+    uint32_t kind;       // instance / problem selector
+    uint32_t pad[2];
+};
+static_assert(sizeof(TaskRecord) == 96, "task record layout");
+
+struct QueueHeader {
+    unsigned long long init_next;   // next initial unit to hand out
+    unsigned long long spawn_head;  // next split item to hand out
+    unsigned long long spawn_tail;  // split items reserved
+    unsigned long long completed;   // work items finished
+    unsigned long long tasks_run;
+    unsigned int error;             // 1: a bounded wait ran out
+    unsigned int pad[5];
+};
+static_assert(sizeof(QueueHeader) == 64, "queue header layout");
+
+uint64_t workspace_bytes(uint64_t capacity);
+
+// One Lunnon map as the batched kernel sees it.
+struct LunnonInstanceDev {
+    uint32_t table_offset;  // into the concatenated next-tables
+    int32_t n;
+    int32_t dim;
+    int32_t start_leaf;
+};
+
+cudaError_t launch_sym_plain(const uint8_t *edges, int start_i, int stop_i, const uint8_t *d_cycles,
+                             uint64_t num, uint64_t *d_counts, uint64_t *d_nodes,
+                             cudaStream_t stream);
+cudaError_t launch_sym_batched(const uint8_t *edges, int start_i, int stop_i,
+                               const uint8_t *d_cycles, uint64_t num, uint64_t *d_counts,
+                               uint64_t *d_nodes, void *d_workspace, const BatchKnobs &knobs,
+                               cudaStream_t stream);
+cudaError_t launch_lunnon_plain(const uint8_t *d_table, int n, int dim, int start_leaf,
+                                const uint8_t *d_states, uint32_t stride, uint64_t num,
+                                uint64_t *d_per_state, uint64_t *d_total, uint64_t *d_nodes,
+                                cudaStream_t stream);
+// Batched multi-instance Lunnon: states of all instances concatenated;
+// d_state_owner[k] = instance of state k; d_counts[instance] += count/leaf.
+cudaError_t launch_lunnon_batched(const uint8_t *d_tables, uint32_t tables_bytes,
+                                  const LunnonInstanceDev *d_inst, int num_inst,
+                                  const uint8_t *d_states, const uint32_t *d_state_owner,
+                                  uint64_t num, uint64_t *d_counts, uint64_t *d_nodes,
+                                  void *d_workspace, const BatchKnobs &knobs, cudaStream_t stream);
+
+int device_sm_count();
+
+}  // namespace mf
+
+#include "sym_expand.inl"

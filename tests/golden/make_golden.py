@@ -1,0 +1,129 @@
+"""Generate tests/golden/reference_counts.json from the reference's own CPU
+solvers, built from source by `make -C oracle ref` into oracle/_ref/.
+
+    python tests/golden/make_golden.py          # needs oracle/_ref/{mf,mf_fast,sym_fold}
+
+Every value in the output was printed by an unmodified reference binary on
+this machine; published values quoted in the reference's documents are kept
+in a separate section with their source lines.  The oracle restatement and
+the GPU engine are both checked against this file.
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+REF = ROOT / "oracle" / "_ref"
+
+
+def run(cmd, env=None):
+    e = dict(os.environ)
+    e.update(env or {})
+    res = subprocess.run([str(c) for c in cmd], capture_output=True, text=True, env=e, check=True)
+    return res.stdout.strip().splitlines()[0].strip()
+
+
+def lunnon_jobs():
+    jobs = []
+    for p in range(2, 7):
+        for q in range(p, 7):
+            if (p, q) == (6, 6):
+                continue  # ~15 min single-threaded; the published value is used
+            jobs.append((f"{p}x{q}", [REF / "mf", p, q]))
+    for k in range(8, 21):
+        jobs.append((f"1x{k}", [REF / "mf", 1, k]))
+    for k in range(1, 6):
+        jobs.append((f"2x2x{k}", [REF / "mf", 2, 2, k]))
+    jobs.append(("1x1", [REF / "mf", 1, 1]))
+    jobs.append(("2x3x4", [REF / "mf", 2, 3, 4]))
+    return jobs
+
+
+def prefix_jobs():
+    out = []
+    for grid, depth in [(4, 8), (5, 12), (5, 15), (6, 12), (6, 18), (7, 18), (7, 23)]:
+        out.append((f"{grid}x{grid}@{depth}", [REF / "mf_fast", grid, depth, 1]))
+    return out
+
+
+def sym_jobs():
+    jobs = []
+    for n in range(1, 7):
+        jobs.append((f"n{n}", [REF / "sym_fold", n, 8], {}))
+    jobs.append(("7x7_d24_first2000", [REF / "sym_fold", 7, 8, 2000, 0], {"MF_STREAM_CASES": "1"}))
+    jobs.append(("7x7_d24_300000+500", [REF / "sym_fold", 7, 8, 500, 300000], {"MF_STREAM_CASES": "1"}))
+    jobs.append(("7x7_d20_first3000", [REF / "sym_fold", 7, 8, 3000, 0],
+                 {"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "20"}))
+    jobs.append(("8x8_d36_first200", [REF / "sym_fold", 8, 8, 200, 0],
+                 {"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "36"}))
+    jobs.append(("8x8_d36_120000000+200", [REF / "sym_fold", 8, 8, 200, 120000000],
+                 {"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "36"}))
+    jobs.append(("8x8_d36_240192700+500", [REF / "sym_fold", 8, 8, 500, 240192700],
+                 {"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "36"}))
+    jobs.append(("8x8_d24_case400000", [REF / "sym_fold", 8, 8, 1, 400000], {"MF_EXPANDED_N": "24"}))
+    jobs.append(("8x8_d30_first300", [REF / "sym_fold", 8, 8, 300, 0],
+                 {"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "30"}))
+    return jobs
+
+
+def setup_jobs():
+    jobs = []
+    for n, e in [(7, 24), (8, 24), (8, 28), (8, 36)]:
+        jobs.append((f"{n}x{n}_d{e}", [REF / "sym_fold", n, 1],
+                     {"MF_EXPANDED_N": str(e), "MF_SETUP_ONLY": "1"}))
+    return jobs
+
+
+PUBLISHED = {
+    "squares": {  # mfah/folding.py:8-17
+        "1": 1, "2": 8, "3": 1368, "4": 300608, "5": 186086600, "6": 123912532224,
+        "7": 129950723279272, "8": 162403827553180928,
+    },
+    "prefix_states": {  # EXPERIMENTS.md:35-47
+        "7x7@18": 293428, "7x7@20": 751142, "7x7@22": 5917082, "7x7@23": 8783910,
+        "8x8@20": 1428966, "8x8@22": 3658148, "8x8@24": 8377532,
+    },
+    "sym_8x8_expanded_cases": {  # EXPERIMENTS.md:65-71
+        "24": 414992, "26": 2512120, "28": 5158056, "30": 9447816, "32": 66351430,
+        "34": 125889268, "36": 240192829,
+    },
+    "sym_8x8_partial_sums": {  # EXPERIMENTS.md:77-81
+        "d24_case100000": 961512726016, "d24_case400000": 39987229696,
+        "d32_first1000": 4354325657600, "d36_first100000": 35390073426944,
+    },
+    "sources": "mfah/folding.py:8-17, EXPERIMENTS.md:35-47,65-71,77-81",
+}
+
+
+def main():
+    for b in ("mf", "mf_fast", "sym_fold"):
+        if not (REF / b).exists():
+            sys.exit(f"missing {REF / b}: run `make -C oracle ref` first")
+    out = {"generated_by": "tests/golden/make_golden.py from oracle/_ref binaries",
+           "lunnon": {}, "prefix_states": {}, "sym": {}, "sym_setup": {},
+           "published": PUBLISHED}
+    with ThreadPoolExecutor(max_workers=os.cpu_count()) as ex:
+        lf = {k: ex.submit(run, cmd) for k, cmd in lunnon_jobs()}
+        pf = {k: ex.submit(run, cmd, {"MF_COLLECT_ONLY": "1"}) for k, cmd in prefix_jobs()}
+        sf = {k: ex.submit(run, cmd, env) for k, cmd, env in sym_jobs()}
+        uf = {k: ex.submit(run, cmd, env) for k, cmd, env in setup_jobs()}
+        for k, f in lf.items():
+            out["lunnon"][k] = int(f.result())
+        for k, f in pf.items():
+            out["prefix_states"][k] = int(f.result())
+        for k, f in sf.items():
+            out["sym"][k] = int(f.result())
+        for k, f in uf.items():
+            out["sym_setup"][k] = int(f.result())
+    (HERE / "reference_counts.json").write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
+    print(json.dumps(out, indent=1, sort_keys=True))
+
+
+if __name__ == "__main__":
+    main()

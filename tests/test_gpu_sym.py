@@ -1,0 +1,167 @@
+"""GPU parity of the sym_fold kernels: per-case counts and node counts
+against the oracle, chunk sums against the reference's own sym_fold output
+(golden), and the WASM solve_cases contract against mfah/folding.py."""
+import json
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_small_squares(engine, cuda, golden, n, mode):
+    assert engine.sym_fold(n, mode=mode) == golden["sym"][f"n{n}"]
+
+
+CHUNKS = [
+    # (golden key, n, expanded_n, max_cases, start_case)
+    ("7x7_d24_first2000", 7, 24, 2000, 0),
+    ("7x7_d24_300000+500", 7, 24, 500, 300000),
+    ("7x7_d20_first3000", 7, 20, 3000, 0),
+    ("8x8_d36_first200", 8, 36, 200, 0),
+    ("8x8_d36_120000000+200", 8, 36, 200, 120000000),
+    ("8x8_d36_240192700+500", 8, 36, 500, 240192700),
+    ("8x8_d24_case400000", 8, 24, 1, 400000),
+    ("8x8_d30_first300", 8, 30, 300, 0),
+]
+
+
+@pytest.mark.parametrize("key,n,e,count,start", CHUNKS)
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_chunks_match_reference(engine, cuda, golden, key, n, e, count, start, mode):
+    assert engine.sym_fold(n, count, start, expanded_n=e, mode=mode) == golden["sym"][key]
+
+
+def _device_counts(engine, torch, n, start_i, stop_i, cycles, mode):
+    d_cyc = torch.from_numpy(np.ascontiguousarray(cycles)).cuda()
+    counts = torch.zeros(len(cycles), dtype=torch.int64, device="cuda")
+    nodes = torch.zeros(1, dtype=torch.int64, device="cuda")
+    if mode == "plain":
+        engine.count_cases_device(n, start_i, stop_i, d_cyc.data_ptr(), len(cycles),
+                                  counts.data_ptr(), nodes.data_ptr())
+    else:
+        ws = torch.empty(engine.sym_workspace_bytes(), dtype=torch.uint8, device="cuda")
+        engine.count_cases_batched_device(n, start_i, stop_i, d_cyc.data_ptr(), len(cycles),
+                                          counts.data_ptr(), ws.data_ptr(), ws.numel(),
+                                          nodes.data_ptr())
+    torch.cuda.synchronize()
+    return counts.cpu().numpy().view(np.uint64), int(nodes.item())
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_per_case_counts_and_nodes_7x7(engine, cuda, orc, mode):
+    plan = engine.SymPlan(7, 24)
+    rng = np.random.default_rng(7)
+    pick = np.sort(rng.choice(plan.total_cases, 600, replace=False))
+    cyc_all, mult_all = plan.cases()
+    cycles = cyc_all[pick]
+    got, nodes = _device_counts(engine, cuda, 7, 24, 49, cycles, mode)
+    total, want, w = orc.sym_count_cases(7, 24, cycles, None, threads=os.cpu_count() or 4)
+    assert (got == want).all()
+    assert nodes == w.nodes  # recurse_count calls, sym_fold.cpp:219
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_partial_depth_counts_8x8(engine, cuda, orc, mode):
+    # stop_i < n*n counts cycles reaching stop_i cells (the expansion index).
+    plan = engine.SymPlan(8, 24)
+    cycles, _ = plan.cases(1000, 300)
+    got, _ = _device_counts(engine, cuda, 8, 24, 30, cycles, mode)
+    want = [orc.sym_count_to(8, c, 24, 30)[0] for c in cycles]
+    assert list(got) == want
+
+
+def test_batched_equals_plain_on_skewed_cases(engine, cuda):
+    # The heaviest 7x7 cases force device-side splits.
+    plan = engine.SymPlan(7, 16)
+    cycles, _ = plan.cases()
+    plain, n1 = _device_counts(engine, cuda, 7, 16, 49, cycles, "plain")
+    batched, n2 = _device_counts(engine, cuda, 7, 16, 49, cycles, "batched")
+    assert (plain == batched).all()
+    assert n1 == n2
+
+
+def test_full_7x7(engine, cuda, golden):
+    ans, st = engine.sym_fold(7, mode="batched", with_stats=True)
+    assert ans == golden["published"]["squares"]["7"]
+    assert st.splits > 0
+
+
+def test_malformed_case_reported(engine, cuda):
+    torch = cuda
+    plan = engine.SymPlan(7, 24)
+    cycles, _ = plan.cases(0, 8)
+    cycles = cycles.copy()
+    cycles[3, 0] = 60  # points outside the placed cells
+    got, _ = _device_counts(engine, torch, 7, 24, 49, cycles, "plain")
+    assert got[3] == np.uint64(2**64 - 1)
+    assert (got[[0, 1, 2, 4]] != np.uint64(2**64 - 1)).all()
+
+
+def _wasm_vectors():
+    return json.loads((ROOT / "tests" / "golden" / "wasm_vectors.json").read_text())
+
+
+@pytest.mark.parametrize("idx", range(3))
+def test_solve_cases_contract(engine, cuda, orc, idx):
+    vec = _wasm_vectors()["cases"][idx]
+    n, depth, stop = vec["n"], vec["depth"], vec["stopDepth"]
+    cycles = np.array(vec["prefix_bytes"], np.uint8)
+    mults = [1] * len(cycles)
+    buf = engine.pack_case_buffer(cycles, mults, n)
+    count, nodes, status = engine.solve_cases(n, depth, stop, buf, len(cycles))
+    assert status == 0
+    assert count == vec["expected"]
+    want_nodes = sum(orc.sym_count_to(n, c, depth, stop)[1].nodes for c in cycles)
+    assert nodes == want_nodes
+
+
+def test_solve_cases_multiplier(engine, cuda, orc):
+    plan = engine.SymPlan(6)
+    cycles, mults = plan.cases(0, 40)
+    buf = engine.pack_case_buffer(cycles, mults, 6)
+    count, nodes, status = engine.solve_cases(6, 16, 36, buf, 40)
+    total, per, w = orc.sym_count_cases(6, 16, cycles, mults, threads=4)
+    assert status == 0 and count == total
+
+
+def _cli(name, *args, env=None):
+    from map_folding_gb300 import build
+
+    e = dict(os.environ)
+    e.update(env or {})
+    return subprocess.run([str(build.BIN / name), *map(str, args)], capture_output=True,
+                          text=True, env=e)
+
+
+def test_sym_fold_cli_stream_chunk(engine, cuda, golden):
+    r = _cli("sym_fold", 8, 16, 200, 0, env={"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "36"})
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip() == str(golden["sym"]["8x8_d36_first200"])
+    assert "stream_seed_cases=1225 stream_from=16 stream_to=36" in r.stderr
+    assert "completed=200" in r.stderr
+    assert "n=8 threads=16 max_cases=200 start_case=0 total_s=" in r.stderr
+
+
+def test_sym_fold_cli_full_6(engine, cuda, golden):
+    for mode in ("plain", "batched"):
+        r = _cli("sym_fold", 6, 4, env={"MF_GPU_MODE": mode})
+        assert r.returncode == 0, r.stderr
+        assert r.stdout.strip() == str(golden["sym"]["n6"])
+        assert "center_cases=9394" in r.stderr and "reduced_cases=1225" in r.stderr
+
+
+def test_gpu_folding_cli(engine, cuda, golden):
+    r = _cli("gpu_folding", 5, 15)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.splitlines() == ["Number of partial states at depth 15: 13416",
+                                     f"Total number of ways: {golden['lunnon']['5x5']}"]
+    r = _cli("gpu_folding", 4, 6, "plain", "3x6")
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.splitlines()[-1] == f"Total number of ways: {golden['lunnon']['3x6']}"
