@@ -1,0 +1,315 @@
+#!/usr/bin/env python
+"""Benchmark: the 7x7 symmetry-reduced full count on one GB300.
+
+Workload (one "step"): count all 433,131 sym_fold cases of the 7x7 map
+expanded to 24 cells (MF_EXPANDED_N=24, the reference default) to
+completion, i.e. the whole 7x7 answer 129950723279272, with the batched
+persistent work-stealing kernel.  Inputs are resident in HBM for `value`;
+`e2e` runs the same count through the C ABI with host buffers (case
+selection, host->device copy, kernel, device->host copy of per-case counts).
+
+Metric: reference DFS nodes per second -- recurse_count calls of
+sym_fold.cpp:219, counted exactly by the kernel (and equal to the oracle's
+count, which the GPU tests check) -- divided by device time.  ms_per_step is
+the 7x7 wall time on the device.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N = 7
+EXPANDED_N = 24
+ANSWER_7X7 = 129950723279272
+METRIC = "7x7 sym_fold count: reference DFS nodes/s (recurse_count calls), batched GPU"
+UNIT = "nodes/s"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int = 0):
+        self.device = device_index
+        self.rows = []
+        self._stop = threading.Event()
+        self._thread = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
+                     "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                for line in out.stdout.strip().splitlines():
+                    self.rows.append([x.strip() for x in line.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._thread = threading.Thread(target=self._run, daemon=True)
+        self._thread.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        self._thread.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def cpu_sample_cases(budget_s: float = 12.0):
+    """A bounded prefix of the 7x7 cases for the CPU legs (about budget_s of
+    work on all host cores)."""
+    from oracle import oracle
+
+    cyc, mult = oracle.sym_expand(N, EXPANDED_N, 0, 0)
+    return cyc, mult
+
+
+def time_cpu(cases, mults, threads, target_s=12.0):
+    """Time the oracle (a restatement of sym_fold.cpp's solver) on growing
+    prefixes of the case list until one run takes ~target_s; returns
+    (nodes/s, sample description, seconds)."""
+    from oracle import oracle
+
+    count = 256
+    while True:
+        t0 = time.perf_counter()
+        _, _, w = oracle.sym_count_cases(N, EXPANDED_N, cases[:count], mults[:count], threads)
+        el = time.perf_counter() - t0
+        if el >= target_s * 0.5 or count >= len(cases):
+            return w.nodes / el, f"first {count} of {len(cases)} 7x7 depth-24 cases", el, count
+        count = min(len(cases), int(count * max(2.0, target_s / max(el, 1e-3))))
+
+
+def run_reference(args):
+    """The reference's CPU solver (oracle restatement of sym_fold.cpp: the
+    reference's binaries cannot be built on this host) on all host threads,
+    a bounded sample per step."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    cases, mults = cpu_sample_cases()
+    rate, sample, el, count = time_cpu(cases, mults, threads, target_s=8.0)
+    from oracle import oracle
+
+    for _ in range(args.warmup):
+        oracle.sym_count_cases(N, EXPANDED_N, cases[:count], mults[:count], threads)
+    times = []
+    nodes = 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, _, w = oracle.sym_count_cases(N, EXPANDED_N, cases[:count], mults[:count], threads)
+        times.append(time.perf_counter() - t0)
+        nodes = w.nodes
+    value = nodes * len(times) / sum(times)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic: the reference's own 7x7 case list (deterministic)",
+        "config": {"workload": f"7x7 sym_fold depth-24 cases, CPU sample ({sample})",
+                   "n": N, "expanded_n": EXPANDED_N, "threads": threads},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import map_folding_gb300 as mf
+    from map_folding_gb300 import build as mfbuild
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if not mfbuild.LIB.exists():
+        mfbuild.build()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    plan = mf.SymPlan(N, EXPANDED_N)
+    cycles, mults = plan.cases()
+    # replicas: every rank counts the whole map (the path shards only by
+    # case ranges across boxes; see the chunk driver)
+    d_cyc = torch.from_numpy(np.ascontiguousarray(cycles)).cuda()
+    d_counts = torch.zeros(len(cycles), dtype=torch.int64, device="cuda")
+    d_nodes = torch.zeros(1, dtype=torch.int64, device="cuda")
+    cfg = None
+    ws = torch.empty(mf.sym_workspace_bytes(cfg), dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    stream = torch.cuda.current_stream()
+    mult_t = torch.from_numpy(mults.astype(np.int64))
+
+    def step():
+        d_nodes.zero_()
+        mf.count_cases_batched_device(N, EXPANDED_N, N * N, d_cyc.data_ptr(), len(cycles),
+                                      d_counts.data_ptr(), ws.data_ptr(), ws.numel(),
+                                      d_nodes.data_ptr(), cfg, stream.cuda_stream)
+
+    def check():
+        c = d_counts.cpu().numpy().view(np.uint64)
+        total = sum(int(m) * int(x) for m, x in zip(mults, c)) * N * N
+        return total
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+    assert check() == ANSWER_7X7, "warm-up count is not bit-exact"
+    nodes_per_step = int(d_nodes.item())
+
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step()
+            b.record(stream)
+            torch.cuda.synchronize()
+            times.append(a.elapsed_time(b) * 1e-3)
+            assert int(d_nodes.item()) == nodes_per_step
+    assert check() == ANSWER_7X7, "timed count is not bit-exact"
+    t_step = sum(times) / len(times)
+    t_max = torch.tensor([sum(times)], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    value = world * nodes_per_step * len(times) / float(t_max.item())
+
+    # End to end through the C ABI with host buffers.
+    e2e_times = []
+    e2e_st = None
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ans, st = plan.solve(0, 0, "batched")
+        e2e_times.append(time.perf_counter() - t0)
+        assert ans == ANSWER_7X7
+        e2e_st = st
+    e2e_value = world * nodes_per_step * len(e2e_times) / sum(e2e_times)
+
+    # The plain one-thread-per-case kernel on the same cases, once.
+    plain_s = None
+    if args.plain:
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        mf.count_cases_device(N, EXPANDED_N, N * N, d_cyc.data_ptr(), len(cycles),
+                              d_counts.data_ptr(), 0, stream.cuda_stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        plain_s = a.elapsed_time(b) * 1e-3
+        assert check() == ANSWER_7X7
+
+    # Roofline: state-load bytes per launch (cases in, counts out) over the
+    # launch time, against measured HBM copy bandwidth.
+    algo_bytes = len(cycles) * (64 + 8)
+    hbm_peak, peak_kind = peaks()
+    achieved = algo_bytes / t_step / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": None,
+                "peak_source": peak_kind,
+                "note": "integer-issue/latency-bound DFS; HBM carries only the case loads"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, sample, el, count = time_cpu(cycles, mults, threads, target_s=10.0)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic: the reference's own 7x7 case list (deterministic)",
+            "config": {"workload": "7x7 full count, sym_fold cases at MF_EXPANDED_N=24 (433131)",
+                       "n": N, "expanded_n": EXPANDED_N, "cases": len(cycles),
+                       "nodes_per_step": nodes_per_step, "l2": "flushed between steps (256 MB write)",
+                       "kernel": "batched persistent work-stealing", "parallelism": "replicas"},
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": int(e2e_st.h2d_bytes) if e2e_st else 0,
+                    "d2h_bytes_per_step": int(e2e_st.d2h_bytes) if e2e_st else 0,
+                    "ms_per_step": 1e3 * sum(e2e_times) / len(e2e_times)},
+            "gpu_launches": args.steps,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "plain_ms_per_step": None if plain_s is None else 1e3 * plain_s,
+            "batched_vs_plain": None if plain_s is None else plain_s / t_step,
+            "splits_per_step": int(e2e_st.splits) if e2e_st else None,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--plain", action="store_true", default=True)
+    ap.add_argument("--no-plain", dest="plain", action="store_false")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

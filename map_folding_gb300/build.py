@@ -74,7 +74,11 @@ def build(force: bool = False, verbose: bool = False) -> Path:
                 print(" ".join(cmd), flush=True)
         list(ex.map(_run, jobs))
     if force or _stale(LIB, objs):
-        _run([cc, "-shared", *ARCH, "-o", str(LIB), *map(str, objs), "-lcudart"])
+        # Link to a temporary name and rename: the linker rewrites an existing
+        # output in place, which would corrupt processes that have it mapped.
+        tmp = LIB.with_suffix(".so.tmp")
+        _run([cc, "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-lcudart"])
+        os.replace(tmp, LIB)
     for name, src in CLI_SOURCES.items():
         o = OBJ / (Path(src).stem + ".o")
         exe = BIN / name

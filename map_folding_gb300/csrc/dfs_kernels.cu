@@ -15,10 +15,11 @@
 //   *_plain_kernel    one thread per unit (prefix state / case), one launch
 //   *_batched_kernel  persistent grid, device work queue, subtree splitting
 //
-// Every walk is bounded by the number of placed items and every device wait
-// by a limit, so malformed input cannot hang a kernel: a unit whose list is
-// inconsistent reports UINT64_MAX (plain) or raises the queue error flag
-// (batched).
+// Every unit's list is checked to be a permutation of its placed items before
+// its search starts, which bounds every walk (see list_valid), and every
+// device wait has a limit, so malformed input cannot hang a kernel: a unit
+// whose list is malformed reports UINT64_MAX (plain) or raises the queue
+// error flag (batched).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -54,13 +55,26 @@ struct List {
     }
 };
 
-// A unit's list is usable only if every placed item points at a placed item;
-// unplaced items are written before they are read.
+// A unit's list is usable only if it is a permutation of the placed items
+// (items >= placed are written before they are read).  That is also what
+// makes every walk below terminate without a step bound: each walk iterates
+// an injective map (the list composed with an involution -- the page's
+// partner matching for sym, the dimension's neighbour table d[l][.] for
+// Lunnon) from a point with no preimage, so it reaches its end in fewer
+// than `placed` + 1 steps.  Insertions keep the list a permutation.
 template <int TPB>
-__device__ __forceinline__ bool list_consistent(const List<TPB> &L, int placed) {
+__device__ __forceinline__ bool list_valid(const List<TPB> &L, int placed) {
     bool ok = true;
-    for (int k = 0; k < placed; ++k) ok &= L.get(k) < placed;
-    return ok;
+    uint64_t seen_lo = 0, seen_hi = 0;
+    for (int k = 0; k < placed; ++k) {
+        const int v = L.get(k);
+        ok &= v < placed;
+        if (v < 64) seen_lo |= 1ULL << v;
+        else seen_hi |= 1ULL << (v & 63);
+    }
+    const uint64_t want_lo = low_bits(placed);
+    const uint64_t want_hi = placed > 64 ? low_bits(placed - 64) : 0;
+    return ok && seen_lo == want_lo && seen_hi == want_hi;
 }
 
 // ------------------------------------------------------------- rules -----
@@ -68,34 +82,38 @@ __device__ __forceinline__ bool list_consistent(const List<TPB> &L, int placed) 
 // sym_fold.cpp:179-204: positions j < i after which cell i may follow in the
 // stack.  For each edge page whose neighbour `other` of i is placed, walk the
 // cycle from `other`, hopping over every placed partner pair, and keep the
-// positions landed on; AND the pages.
+// positions landed on; AND the pages.  The pages' walks run as one flat loop
+// (a lane moves on to its next page inside the same loop), so a warp waits
+// for its longest lane's total walk, not for the sum of per-page maxima.
 struct SymRules {
     const uint8_t *edge;  // 4 pages x 64, shared memory
     template <int TPB>
     __device__ __forceinline__ uint64_t gaps(const List<TPB> &L, int i, unsigned long long &nodes,
-                                             bool &bad) const {
+                                             bool &) const {
         ++nodes;
         uint64_t good = low_bits(i);
-#pragma unroll 1
-        for (int p = 0; p < 4; ++p) {
-            const uint8_t *e = edge + p * kSymCells;
-            const int other = e[i];
-            if (other >= i) continue;
-            uint64_t allowed = 1ULL << other;
-            int j = L.get(other);
-            int guard = i;
-            while (j != other) {
-                const int partner = e[j];
-                j = partner < i ? partner : j;
-                allowed |= 1ULL << j;
-                j = L.get(j);
-                if (--guard < 0) {
-                    bad = true;
-                    return 0;
-                }
+        unsigned pend = 0;  // pages whose neighbour of i is placed
+#pragma unroll
+        for (int p = 0; p < 4; ++p) pend |= unsigned(edge[p * kSymCells + i] < i) << p;
+        const uint8_t *e = edge;
+        uint64_t allowed = ~0ULL;
+        int other = 0, j = 0;
+        for (;;) {
+            if (j == other) {  // current page finished (or none started)
+                good &= allowed;
+                if (!good || !pend) break;
+                const int p = __ffs(pend) - 1;
+                pend &= pend - 1;
+                e = edge + p * kSymCells;
+                other = e[i];
+                allowed = 1ULL << other;
+                j = L.get(other);
+                continue;
             }
-            good &= allowed;
-            if (!good) break;
+            const int partner = e[j];
+            j = partner < i ? partner : j;
+            allowed |= 1ULL << j;
+            j = L.get(j);
         }
         return good;
     }
@@ -108,34 +126,37 @@ struct SymRules {
 // position 0..l-1 is a gap.  Position 0 (insert on top of the sentinel) is
 // dropped for l >= 2: it makes b[0] = l != 1 and the normal-form filter
 // (mf.c:83) would prune the whole subtree.  `nodes` counts the insertions
-// the reference loop would make (mf.c:136-142), position 0 included.
+// the reference loop would make (mf.c:136-142), position 0 included.  As for
+// sym, the dimensions' walks run as one flat loop.
 struct LunnonRules {
     const uint8_t *table;  // [dim][n+1][n+1]
     int n;
     int dim;
     template <int TPB>
     __device__ __forceinline__ uint64_t gaps(const List<TPB> &L, int l, unsigned long long &nodes,
-                                             bool &bad) const {
+                                             bool &) const {
         const int w = n + 1;
-        uint64_t mask = ~0ULL;
-        int bound = 0;
-        for (int i = 0; i < dim; ++i) {
-            const uint8_t *row = table + (i * w + l) * w;
-            int m = row[l];
-            if (m == l) continue;
-            ++bound;
-            uint64_t walked = 0;
-            int guard = l;
-            do {
-                walked |= 1ULL << m;
-                m = row[L.get(m)];
-                if (--guard < 0) {
-                    bad = true;
-                    return 0;
+        uint64_t mask = ~0ULL, walked = ~0ULL;
+        int bound = 0, d = -1, m = l;
+        const uint8_t *row = table;
+        for (;;) {
+            if (m == l) {  // current dimension finished (or none started)
+                mask &= walked;
+                if (!mask) break;
+                int first = l;
+                while (++d < dim) {
+                    row = table + (d * w + l) * w;
+                    first = row[l];
+                    if (first != l) break;
                 }
-            } while (m != l);
-            mask &= walked;
-            if (!mask) break;
+                if (d >= dim) break;
+                ++bound;
+                m = first;
+                walked = 0;
+                continue;
+            }
+            walked |= 1ULL << m;
+            m = row[L.get(m)];
         }
         if (!bound) mask = low_bits(l);
         nodes += __popcll(mask);
@@ -257,7 +278,7 @@ __global__ void __launch_bounds__(TPB)
     if (active) {
         const SymRules R{reinterpret_cast<const uint8_t *>(s_edge)};
         Stack S;
-        bool bad = !list_consistent(L, start_i);
+        bool bad = !list_valid(L, start_i);
         unsigned long long leaves = 0;
         const int last = stop_i - 1;
         if (!bad && dfs_begin(R, L, S, start_i, last, leaves, nodes, bad)) {
@@ -297,7 +318,7 @@ __global__ void __launch_bounds__(TPB)
     if (active) {
         const LunnonRules R{s_table, n, dim};
         Stack S;
-        bool bad = !list_consistent(L, start_leaf < n + 1 ? start_leaf : n + 1);
+        bool bad = !list_valid(L, start_leaf < n + 1 ? start_leaf : n + 1);
         if (!bad && dfs_begin(R, L, S, start_leaf, n, leaves, nodes, bad)) {
             int lvl = start_leaf;
             while (!dfs_run(R, L, S, lvl, start_leaf, n, leaves, nodes, 0xffffffffu, bad)) {
@@ -496,7 +517,7 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables, const S
                     owner = uint32_t(k);
                     root = sym.start_i;
                     last = sym.last;
-                    bad = !list_consistent(L, root);
+                    bad = !list_valid(L, root);
                 } else {
                     load_list<TPB, WORDS>(L, lun.states + k * lun.stride, lun.stride);
                     owner = lun.state_owner[k];
@@ -504,7 +525,7 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables, const S
                     lrules = LunnonRules{s_tables + I.table_offset, I.n, I.dim};
                     root = I.start_leaf;
                     last = I.n;
-                    bad = !list_consistent(L, root < I.n + 1 ? root : I.n + 1);
+                    bad = !list_valid(L, root < I.n + 1 ? root : I.n + 1);
                 }
                 if (bad) {
                     flush();

@@ -47,9 +47,10 @@ bool build_lunnon_tables(const int32_t *dims, int ndim, LunnonTables &t, std::st
 inline uint32_t lunnon_state_stride(int n) { return uint32_t((n + 1 + 15) / 16 * 16); }
 
 // Prefix states at leaf depth `depth` in the reference's emission order.
-// Writes up to cap records of `stride` bytes; returns the total count.
+// Writes the records with index in [first, first + cap), `stride` bytes
+// each; returns the total number of states.
 uint64_t collect_lunnon_states(const LunnonTables &t, int depth, uint8_t *out, uint64_t cap,
-                               uint32_t stride);
+                               uint32_t stride, uint64_t first = 0);
 
 // A sensible default split depth for a map with n leaves.
 int default_lunnon_depth(const LunnonTables &t);

@@ -138,7 +138,7 @@ void compute_frame(const LunnonTables &t, const uint8_t *b, int l, GapFrame &f, 
 }  // namespace
 
 uint64_t collect_lunnon_states(const LunnonTables &t, int depth, uint8_t *out, uint64_t cap,
-                               uint32_t stride) {
+                               uint32_t stride, uint64_t first) {
     const int n = t.n;
     if (depth < 0) depth = 0;
     if (depth > n) depth = n;
@@ -153,8 +153,8 @@ uint64_t collect_lunnon_states(const LunnonTables &t, int depth, uint8_t *out, u
         f.count = f.left = 0;
         if (l >= 2 && b[0] != 1) return;  // normal-form filter, mf.c:83
         if (l > depth) {
-            if (found < cap && out != nullptr) {
-                uint8_t *rec = out + found * stride;
+            if (out != nullptr && found >= first && found - first < cap) {
+                uint8_t *rec = out + (found - first) * stride;
                 std::memset(rec, 0, stride);
                 std::memcpy(rec, b, size_t(n) + 1);
             }

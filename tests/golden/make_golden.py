@@ -58,8 +58,8 @@ def sym_jobs():
         jobs.append((f"n{n}", [REF / "sym_fold", n, 8], {}))
     jobs.append(("7x7_d24_first2000", [REF / "sym_fold", 7, 8, 2000, 0], {"MF_STREAM_CASES": "1"}))
     jobs.append(("7x7_d24_300000+500", [REF / "sym_fold", 7, 8, 500, 300000], {"MF_STREAM_CASES": "1"}))
-    jobs.append(("7x7_d20_first3000", [REF / "sym_fold", 7, 8, 3000, 0],
-                 {"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "20"}))
+    jobs.append(("7x7_d28_first2000", [REF / "sym_fold", 7, 8, 2000, 0],
+                 {"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "28"}))
     jobs.append(("8x8_d36_first200", [REF / "sym_fold", 8, 8, 200, 0],
                  {"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "36"}))
     jobs.append(("8x8_d36_120000000+200", [REF / "sym_fold", 8, 8, 200, 120000000],
@@ -67,8 +67,8 @@ def sym_jobs():
     jobs.append(("8x8_d36_240192700+500", [REF / "sym_fold", 8, 8, 500, 240192700],
                  {"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "36"}))
     jobs.append(("8x8_d24_case400000", [REF / "sym_fold", 8, 8, 1, 400000], {"MF_EXPANDED_N": "24"}))
-    jobs.append(("8x8_d30_first300", [REF / "sym_fold", 8, 8, 300, 0],
-                 {"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "30"}))
+    jobs.append(("8x8_d32_first100", [REF / "sym_fold", 8, 8, 100, 0],
+                 {"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "32"}))
     return jobs
 
 

@@ -23,12 +23,12 @@ CHUNKS = [
     # (golden key, n, expanded_n, max_cases, start_case)
     ("7x7_d24_first2000", 7, 24, 2000, 0),
     ("7x7_d24_300000+500", 7, 24, 500, 300000),
-    ("7x7_d20_first3000", 7, 20, 3000, 0),
+    ("7x7_d28_first2000", 7, 28, 2000, 0),
     ("8x8_d36_first200", 8, 36, 200, 0),
     ("8x8_d36_120000000+200", 8, 36, 200, 120000000),
     ("8x8_d36_240192700+500", 8, 36, 500, 240192700),
     ("8x8_d24_case400000", 8, 24, 1, 400000),
-    ("8x8_d30_first300", 8, 30, 300, 0),
+    ("8x8_d32_first100", 8, 32, 100, 0),
 ]
 
 
@@ -78,11 +78,11 @@ def test_partial_depth_counts_8x8(engine, cuda, orc, mode):
 
 
 def test_batched_equals_plain_on_skewed_cases(engine, cuda):
-    # The heaviest 7x7 cases force device-side splits.
-    plan = engine.SymPlan(7, 16)
+    # 1225 6x6 representatives of very uneven size force device-side splits.
+    plan = engine.SymPlan(6)
     cycles, _ = plan.cases()
-    plain, n1 = _device_counts(engine, cuda, 7, 16, 49, cycles, "plain")
-    batched, n2 = _device_counts(engine, cuda, 7, 16, 49, cycles, "batched")
+    plain, n1 = _device_counts(engine, cuda, 6, 16, 36, cycles, "plain")
+    batched, n2 = _device_counts(engine, cuda, 6, 16, 36, cycles, "batched")
     assert (plain == batched).all()
     assert n1 == n2
 

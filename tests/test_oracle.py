@@ -74,10 +74,10 @@ def test_sym_setup_counts(orc, golden):
 def test_sym_chunks(orc, golden):
     got, _ = orc.sym_solve(8, THREADS, max_cases=200, start_case=0, expanded_n=36)
     assert got == golden["sym"]["8x8_d36_first200"]
-    got, _ = orc.sym_solve(7, THREADS, max_cases=3000, start_case=0, expanded_n=20)
-    assert got == golden["sym"]["7x7_d20_first3000"]
-    got, _ = orc.sym_solve(8, THREADS, max_cases=300, start_case=0, expanded_n=30)
-    assert got == golden["sym"]["8x8_d30_first300"]
+    got, _ = orc.sym_solve(7, THREADS, max_cases=2000, start_case=0, expanded_n=28)
+    assert got == golden["sym"]["7x7_d28_first2000"]
+    got, _ = orc.sym_solve(8, THREADS, max_cases=100, start_case=0, expanded_n=32)
+    assert got == golden["sym"]["8x8_d32_first100"]
 
 
 def test_wasm_vectors(orc):
