@@ -61,13 +61,13 @@ typedef struct {
 /* Launch shape and scheduling knobs of the persistent (batched) kernels.
  * Zero in any field selects the built-in default. */
 typedef struct {
-    uint32_t block_threads;  /* threads per CTA (multiple of 32) */
-    uint32_t blocks_per_sm;  /* resident CTAs per SM for the persistent grid */
-    uint32_t node_budget;    /* DFS nodes a thread runs between split checks */
-    uint32_t hungry_factor;  /* split while queued work < factor x threads */
-    uint64_t queue_capacity; /* device work-item slots for split subtrees */
-    uint32_t wait_limit;     /* bound on each device-side spin wait */
-    uint32_t reserved;
+    uint32_t block_threads;  /* threads per CTA: 128 or 256 */
+    uint32_t blocks_per_sm;  /* resident CTAs per SM (0: as many as fit) */
+    uint32_t node_budget;    /* lockstep rounds (one node each) between split checks */
+    uint32_t hungry_factor;  /* split while queued items < factor/8 x threads */
+    uint64_t queue_capacity; /* split-item ring cells (rounded up to a power of 2) */
+    uint32_t wait_limit;     /* idle rounds before an idle warp leaves */
+    uint32_t stack_mode;     /* 0: DFS stack in shared memory when it fits, 1: local */
 } mf_batch_config;
 
 /* ======================================================================
@@ -116,6 +116,14 @@ int32_t mf_lunnon_count_states(const mf_lunnon_plan *plan, int32_t start_leaf,
 int32_t mf_lunnon_count(const mf_lunnon_plan *plan, int32_t depth, int32_t mode,
                         const mf_batch_config *cfg, uint64_t *count_out,
                         uint64_t *states_out, mf_run_stats *stats);
+
+/* As mf_lunnon_count, over prefix states [first_state, first_state +
+ * max_states) of the emission order only (max_states 0: to the end): the
+ * partial count of those subtrees.  What `gpu_folding_v2 grid depth ...
+ * max_states` computes (gpu_folding_v2.cu:258-325 stops after max_states). */
+int32_t mf_lunnon_count_range(const mf_lunnon_plan *plan, int32_t depth, uint64_t first_state,
+                              uint64_t max_states, int32_t mode, const mf_batch_config *cfg,
+                              uint64_t *count_out, uint64_t *states_out, mf_run_stats *stats);
 
 /* Batched uneven launch: all prefix states of `num_plans` maps (each at its
  * own depth) in ONE persistent work-stealing kernel that splits subtrees on

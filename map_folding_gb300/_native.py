@@ -53,7 +53,7 @@ class BatchConfig(ctypes.Structure):
         ("hungry_factor", ctypes.c_uint32),
         ("queue_capacity", ctypes.c_uint64),
         ("wait_limit", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("stack_mode", ctypes.c_uint32),
     ]
 
 
@@ -74,6 +74,7 @@ SIGNATURES = {
     "mf_lunnon_collect": ([_p, _i32, _p, _u64, _pu64], _i32),
     "mf_lunnon_count_states": ([_p, _i32, _p, _u64, _p, _p, _p, _p], _i32),
     "mf_lunnon_count": ([_p, _i32, _i32, _p, _pu64, _pu64, _p], _i32),
+    "mf_lunnon_count_range": ([_p, _i32, _u64, _u64, _i32, _p, _pu64, _pu64, _p], _i32),
     "mf_lunnon_batch_count": ([_p, _i32, _p, _p, _p, _p], _i32),
     "mf_sym_edges": ([_i32, _p], _i32),
     "mf_sym_plan_create": ([_i32, _i32, ctypes.POINTER(_p)], _i32),

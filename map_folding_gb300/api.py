@@ -108,6 +108,18 @@ class LunnonPlan:
                                              ctypes.byref(st)))
         return total.value, states.value, st
 
+    def count_range(self, depth: int, first_state: int = 0, max_states: int = 0,
+                    mode: str | int = "batched", cfg=None):
+        """(partial count, states counted, RunStats) over a range of the
+        prefix states' emission order."""
+        total = ctypes.c_uint64()
+        states = ctypes.c_uint64()
+        st = RunStats()
+        check(_native.load().mf_lunnon_count_range(self._h, depth, first_state, max_states,
+                                                   _mode(mode), _cfg(cfg), ctypes.byref(total),
+                                                   ctypes.byref(states), ctypes.byref(st)))
+        return total.value, states.value, st
+
 
 def gpu_folding(grid_size: int, partition_depth: int, mode: str | int = "batched",
                 dims: Sequence[int] | None = None):

@@ -26,7 +26,8 @@ BIN = PKG / "bin"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include")]
 LIB_SOURCES = ["host.cpp", "capi.cpp", "dfs_kernels.cu"]
-CLI_SOURCES = {"gpu_folding": "cli_gpu_folding.cpp", "sym_fold": "cli_sym_fold.cpp"}
+CLI_SOURCES = {"gpu_folding": "cli_gpu_folding.cpp", "gpu_folding_v2": "cli_gpu_folding_v2.cpp",
+               "sym_fold": "cli_sym_fold.cpp"}
 
 
 def nvcc() -> str:

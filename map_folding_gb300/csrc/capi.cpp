@@ -15,13 +15,15 @@ namespace mf {
 BatchKnobs resolve_knobs(const mf_batch_config *cfg) {
     BatchKnobs k;
     k.block_threads = 128;
-    k.blocks_per_sm = 8;
-    k.node_budget = 128;
+    k.blocks_per_sm = 0;  // as many as fit (occupancy calculator)
+    k.node_budget = 64;
     k.hungry_factor = 2;
-    k.queue_capacity = 1ULL << 20;
+    k.queue_capacity = 1ULL << 16;
     k.wait_limit = 1u << 20;
+    k.stack_mode = 0;
     if (cfg) {
-        if (cfg->block_threads == 64 || cfg->block_threads == 128 || cfg->block_threads == 256)
+        k.stack_mode = cfg->stack_mode;
+        if (cfg->block_threads == 128 || cfg->block_threads == 256)
             k.block_threads = int(cfg->block_threads);
         if (cfg->blocks_per_sm) k.blocks_per_sm = int(std::min<uint32_t>(cfg->blocks_per_sm, 32));
         if (cfg->node_budget) k.node_budget = cfg->node_budget;
@@ -29,6 +31,10 @@ BatchKnobs resolve_knobs(const mf_batch_config *cfg) {
         if (cfg->queue_capacity) k.queue_capacity = cfg->queue_capacity;
         if (cfg->wait_limit) k.wait_limit = cfg->wait_limit;
     }
+    // The split ring indexes cells by ticket & (capacity - 1).
+    uint64_t cap = 16;
+    while (cap < k.queue_capacity && cap < (1ULL << 26)) cap <<= 1;
+    k.queue_capacity = cap;
     return k;
 }
 
@@ -77,6 +83,28 @@ int ensure_device() {
         return MF_ERR_NO_DEVICE;
     }
     return MF_OK;
+}
+
+// Edge pages of each board size, uploaded once per device.
+std::mutex g_edges_mu;
+uint8_t *g_edges[16][9] = {};
+
+const uint8_t *device_edges(int n) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16 || n < 1 || n > 8) return nullptr;
+    std::lock_guard<std::mutex> lock(g_edges_mu);
+    if (!g_edges[dev][n]) {
+        uint8_t host[4 * kSymCells];
+        sym_edges(n, host);
+        uint8_t *d = nullptr;
+        if (cudaMalloc(&d, sizeof(host)) != cudaSuccess) return nullptr;
+        if (cudaMemcpy(d, host, sizeof(host), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaFree(d);
+            return nullptr;
+        }
+        g_edges[dev][n] = d;
+    }
+    return g_edges[dev][n];
 }
 
 struct Timer {
@@ -203,12 +231,19 @@ int32_t mf_lunnon_count_states(const mf_lunnon_plan *cplan, int32_t start_leaf,
 }
 
 static int32_t lunnon_batch_impl(const mf_lunnon_plan *const *plans, int32_t num_plans,
-                                 const int32_t *depths, const mf_batch_config *cfg,
+                                 const int32_t *depths, const uint64_t *firsts,
+                                 const uint64_t *limits, const mf_batch_config *cfg,
                                  uint64_t *counts_out, mf_run_stats *stats);
 
-int32_t mf_lunnon_count(const mf_lunnon_plan *cplan, int32_t depth, int32_t mode,
+int32_t mf_lunnon_count(const mf_lunnon_plan *plan, int32_t depth, int32_t mode,
                         const mf_batch_config *cfg, uint64_t *count_out, uint64_t *states_out,
                         mf_run_stats *stats) {
+    return mf_lunnon_count_range(plan, depth, 0, 0, mode, cfg, count_out, states_out, stats);
+}
+
+int32_t mf_lunnon_count_range(const mf_lunnon_plan *cplan, int32_t depth, uint64_t first_state,
+                              uint64_t max_states, int32_t mode, const mf_batch_config *cfg,
+                              uint64_t *count_out, uint64_t *states_out, mf_run_stats *stats) {
     clear_error();
     auto *plan = const_cast<mf_lunnon_plan *>(cplan);
     if (!plan || !count_out) {
@@ -223,8 +258,10 @@ int32_t mf_lunnon_count(const mf_lunnon_plan *cplan, int32_t depth, int32_t mode
     if (mode == 1) {
         const mf_lunnon_plan *one[1] = {plan};
         int32_t d[1] = {depth};
-        int rc = lunnon_batch_impl(one, 1, d, cfg, count_out, stats);
-        if (rc == MF_OK && states_out) *states_out = stats ? stats->units : 0;
+        mf_run_stats local{};
+        mf_run_stats *st = stats ? stats : &local;
+        int rc = lunnon_batch_impl(one, 1, d, &first_state, &max_states, cfg, count_out, st);
+        if (rc == MF_OK && states_out) *states_out = st->units;
         return rc;
     }
     int rc = ensure_device();
@@ -233,10 +270,12 @@ int32_t mf_lunnon_count(const mf_lunnon_plan *cplan, int32_t depth, int32_t mode
     if (rc) return rc;
     const double t0 = now_seconds();
     const uint32_t stride = lunnon_state_stride(plan->t.n);
-    const uint64_t total = collect_lunnon_states(plan->t, depth, nullptr, 0, stride);
+    const uint64_t all = collect_lunnon_states(plan->t, depth, nullptr, 0, stride);
+    uint64_t total = all > first_state ? all - first_state : 0;
+    if (max_states && max_states < total) total = max_states;
     auto *h_states = static_cast<uint8_t *>(scratch(kHostUnits, total * stride, true));
     if (!h_states) return MF_ERR_CUDA;
-    collect_lunnon_states(plan->t, depth, h_states, total, stride);
+    collect_lunnon_states(plan->t, depth, h_states, total, stride, first_state);
     const double t1 = now_seconds();
     auto *d_states = static_cast<uint8_t *>(scratch(kDevUnits, total * stride, false));
     auto *d_acc = static_cast<uint64_t *>(scratch(kDevCounts, 2 * sizeof(uint64_t), false));
@@ -275,7 +314,8 @@ int32_t mf_lunnon_count(const mf_lunnon_plan *cplan, int32_t depth, int32_t mode
 }
 
 static int32_t lunnon_batch_impl(const mf_lunnon_plan *const *plans, int32_t num_plans,
-                                 const int32_t *depths, const mf_batch_config *cfg,
+                                 const int32_t *depths, const uint64_t *firsts,
+                                 const uint64_t *limits, const mf_batch_config *cfg,
                                  uint64_t *counts_out, mf_run_stats *stats) {
     if (!plans || num_plans < 1 || !counts_out) {
         set_error("plans, num_plans >= 1 and counts_out are required");
@@ -288,7 +328,7 @@ static int32_t lunnon_batch_impl(const mf_lunnon_plan *const *plans, int32_t num
     // Concatenate tables and states of all maps.
     std::vector<LunnonInstanceDev> inst(num_plans);
     std::vector<uint8_t> tables;
-    std::vector<uint64_t> per_plan(num_plans);
+    std::vector<uint64_t> per_plan(num_plans), first(num_plans, 0);
     uint64_t total = 0;
     for (int k = 0; k < num_plans; ++k) {
         const mf_lunnon_plan *p = plans[k];
@@ -305,7 +345,10 @@ static int32_t lunnon_batch_impl(const mf_lunnon_plan *const *plans, int32_t num
         inst[k].start_leaf = d + 1;
         tables.insert(tables.end(), p->t.next.begin(), p->t.next.end());
         tables.resize((tables.size() + 15) / 16 * 16, 0);
-        per_plan[k] = collect_lunnon_states(p->t, d, nullptr, 0, stride);
+        const uint64_t all = collect_lunnon_states(p->t, d, nullptr, 0, stride);
+        first[k] = firsts ? firsts[k] : 0;
+        per_plan[k] = all > first[k] ? all - first[k] : 0;
+        if (limits && limits[k] && limits[k] < per_plan[k]) per_plan[k] = limits[k];
         total += per_plan[k];
     }
     if (tables.size() > 160 * 1024) {
@@ -321,7 +364,7 @@ static int32_t lunnon_batch_impl(const mf_lunnon_plan *const *plans, int32_t num
     uint64_t at = 0;
     for (int k = 0; k < num_plans; ++k) {
         collect_lunnon_states(plans[k]->t, inst[k].start_leaf - 1, h_units + at * stride,
-                              per_plan[k], stride);
+                              per_plan[k], stride, first[k]);
         for (uint64_t s = 0; s < per_plan[k]; ++s) h_owner[at + s] = uint32_t(k);
         at += per_plan[k];
     }
@@ -346,7 +389,10 @@ static int32_t lunnon_batch_impl(const mf_lunnon_plan *const *plans, int32_t num
     MF_TRY_CUDA(cudaMemsetAsync(d_counts + num_plans, 0, 8, st));
     cudaEventRecord(th.b, st);
     cudaEventRecord(tk.a, st);
-    MF_TRY_CUDA(launch_lunnon_batched(d_meta, uint32_t(tables.size()), d_inst, num_plans, d_units,
+    int max_levels = 0;
+    for (const auto &I : inst) max_levels = std::max(max_levels, I.n - I.start_leaf);
+    MF_TRY_CUDA(launch_lunnon_batched(d_meta, uint32_t(tables.size()), d_inst, num_plans,
+                                      max_levels, d_units,
                                       reinterpret_cast<uint32_t *>(d_units + unit_bytes), total,
                                       d_counts, d_counts + num_plans, d_work, knobs, st));
     cudaEventRecord(tk.b, st);
@@ -383,7 +429,7 @@ int32_t mf_lunnon_batch_count(const mf_lunnon_plan *const *plans, int32_t num_pl
                               const int32_t *depths, const mf_batch_config *cfg,
                               uint64_t *counts_out, mf_run_stats *stats) {
     clear_error();
-    return lunnon_batch_impl(plans, num_plans, depths, cfg, counts_out, stats);
+    return lunnon_batch_impl(plans, num_plans, depths, nullptr, nullptr, cfg, counts_out, stats);
 }
 
 // ---------------------------------------------------------------- sym ----
@@ -476,8 +522,11 @@ int32_t mf_sym_count_cases(int32_t n, int32_t start_i, int32_t stop_i, const uin
         set_error("d_cycles must be 16-byte aligned");
         return MF_ERR_ARG;
     }
-    uint8_t edges[4 * kSymCells];
-    sym_edges(n, edges);
+    const uint8_t *edges = device_edges(n);
+    if (!edges) {
+        set_error("uploading the edge pages failed");
+        return MF_ERR_CUDA;
+    }
     MF_TRY_CUDA(launch_sym_plain(edges, start_i, stop_i, d_cycles, num_cases, d_counts, d_nodes,
                                  static_cast<cudaStream_t>(stream)));
     return MF_OK;
@@ -512,8 +561,11 @@ int32_t mf_sym_count_cases_batched(int32_t n, int32_t start_i, int32_t stop_i,
         set_error("at most 2^32-1 cases per call");
         return MF_ERR_ARG;
     }
-    uint8_t edges[4 * kSymCells];
-    sym_edges(n, edges);
+    const uint8_t *edges = device_edges(n);
+    if (!edges) {
+        set_error("uploading the edge pages failed");
+        return MF_ERR_CUDA;
+    }
     MF_TRY_CUDA(launch_sym_batched(edges, start_i, stop_i, d_cycles, num_cases, d_counts, d_nodes,
                                    d_workspace, knobs, static_cast<cudaStream_t>(stream)));
     return MF_OK;
@@ -535,8 +587,11 @@ int count_cases_host(int n, int start_i, int stop_i, const uint8_t *h_cycles, ui
     void *d_work = mode == 1 ? scratch(kDevWork, workspace_bytes(knobs.queue_capacity), false) : nullptr;
     auto *h_hdr = static_cast<uint8_t *>(scratch(kHostCounts, 256, true));
     if (!d_cycles || !d_counts || (mode == 1 && !d_work) || !h_hdr) return MF_ERR_CUDA;
-    uint8_t edges[4 * kSymCells];
-    sym_edges(n, edges);
+    const uint8_t *edges = device_edges(n);
+    if (!edges) {
+        set_error("uploading the edge pages failed");
+        return MF_ERR_CUDA;
+    }
     cudaStream_t s = nullptr;
     Timer th, tk, td;
     cudaEventRecord(th.a, s);

@@ -7,8 +7,9 @@
 // positions recomputed at every level by walking the list.  The engine below
 // keeps that list per thread in shared memory (byte per item, word-interleaved
 // across the CTA so a warp never has a bank conflict), keeps the per-level
-// choices as a 64-bit mask stack instead of the reference's gap[] array, and
-// counts the last level with a popcount.  Gap rules:
+// choices as a 64-bit mask stack (in shared memory when the search is at most
+// kSmemLevels deep, else in local memory) instead of the reference's gap[]
+// array, and counts the last level with a popcount.  Gap rules:
 //   LunnonRules  -- mf.c:88-124 as a bitwise AND of per-dimension walk masks
 //   SymRules     -- sym_fold.cpp:179-204 (get_good)
 // Kernels:
@@ -16,13 +17,15 @@
 //   *_batched_kernel  persistent grid, device work queue, subtree splitting
 //
 // Every unit's list is checked to be a permutation of its placed items before
-// its search starts, which bounds every walk (see list_valid), and every
-// device wait has a limit, so malformed input cannot hang a kernel: a unit
-// whose list is malformed reports UINT64_MAX (plain) or raises the queue
-// error flag (batched).
+// its search starts, which bounds every walk (see list_valid); the device
+// queue is non-blocking (no thread ever waits on another), so malformed input
+// cannot hang a kernel: a unit whose list is malformed reports UINT64_MAX
+// (plain) or raises the queue error flag (batched).
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdlib>
+#include <cstring>
 
 #include "engine.hpp"
 
@@ -30,16 +33,16 @@ namespace mf {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kMaxLevels = 66;      // levels 0..65 (Lunnon up to n + 1 = 65)
-constexpr int kMinSplitHeight = 3;  // never hand out subtrees shallower than this
+constexpr int kLocalLevels = 66;    // local-memory stack: levels 0..65
+constexpr int kMinSplitHeight = 4;  // never hand out subtrees shallower than this
 
 __device__ __forceinline__ uint64_t low_bits(int k) {
     return k >= 64 ? ~0ULL : ((1ULL << k) - 1ULL);
 }
 
-// Per-thread successor list in shared memory.  Byte j of thread t lives in
+// Per-thread byte array in shared memory.  Byte j of thread t lives in
 // 32-bit word (j/4)*TPB + t, so a warp's 32 lanes always address 32
-// different banks, whatever items they touch.
+// different banks, whatever indices they touch.
 template <int TPB>
 struct List {
     uint8_t *base;  // smem + 4 * threadIdx.x
@@ -88,8 +91,8 @@ __device__ __forceinline__ bool list_valid(const List<TPB> &L, int placed) {
 struct SymRules {
     const uint8_t *edge;  // 4 pages x 64, shared memory
     template <int TPB>
-    __device__ __forceinline__ uint64_t gaps(const List<TPB> &L, int i, unsigned long long &nodes,
-                                             bool &) const {
+    __device__ __forceinline__ uint64_t gaps(const List<TPB> &L, int i,
+                                             unsigned long long &nodes) const {
         ++nodes;
         uint64_t good = low_bits(i);
         unsigned pend = 0;  // pages whose neighbour of i is placed
@@ -133,8 +136,8 @@ struct LunnonRules {
     int n;
     int dim;
     template <int TPB>
-    __device__ __forceinline__ uint64_t gaps(const List<TPB> &L, int l, unsigned long long &nodes,
-                                             bool &) const {
+    __device__ __forceinline__ uint64_t gaps(const List<TPB> &L, int l,
+                                             unsigned long long &nodes) const {
         const int w = n + 1;
         uint64_t mask = ~0ULL, walked = ~0ULL;
         int bound = 0, d = -1, m = l;
@@ -165,69 +168,82 @@ struct LunnonRules {
     }
 };
 
-// ---------------------------------------------------------- DFS core -----
+// ------------------------------------------------------------- stacks ----
 
-struct Stack {
-    uint64_t mask[kMaxLevels];   // untried positions per level
-    uint8_t chosen[kMaxLevels];  // position the level's item was inserted after
+// Per-level search state: the untried positions (mask) and the position the
+// level's item was inserted after (chosen).  Levels are stored relative to
+// `base`, the unit's first level.
+template <int TPB, int LEVELS>
+struct SmemStack {
+    static constexpr int kLevels = LEVELS;
+    uint64_t *mask;  // &s_mask[threadIdx.x], level k at mask[k * TPB]
+    List<TPB> chosen;
+    int base;
+    __device__ __forceinline__ uint64_t get(int lvl) const { return mask[(lvl - base) * TPB]; }
+    __device__ __forceinline__ void set(int lvl, uint64_t v) const { mask[(lvl - base) * TPB] = v; }
+    __device__ __forceinline__ int pick(int lvl) const { return chosen.get(lvl - base); }
+    __device__ __forceinline__ void set_pick(int lvl, int j) const { chosen.put(lvl - base, j); }
 };
 
-// Advance one unit's search by at most `budget` gap evaluations.  On entry
-// items root..lvl-1 are inserted and mask[lvl] holds lvl's untried
-// positions.  The last level is never entered: its positions are counted.
-// Returns true when the unit's subtree is exhausted.
-template <class Rules, int TPB>
-__device__ __forceinline__ bool dfs_run(const Rules &R, const List<TPB> &L, Stack &S, int &lvl,
-                                        int root, int last, unsigned long long &leaves,
-                                        unsigned long long &nodes, uint32_t budget, bool &bad) {
+struct LocalStack {
+    static constexpr int kLevels = kLocalLevels;
+    uint64_t mask[kLocalLevels];
+    uint8_t chosen[kLocalLevels];
+    int base;
+    __device__ __forceinline__ uint64_t get(int lvl) const { return mask[lvl - base]; }
+    __device__ __forceinline__ void set(int lvl, uint64_t v) { mask[lvl - base] = v; }
+    __device__ __forceinline__ int pick(int lvl) const { return chosen[lvl - base]; }
+    __device__ __forceinline__ void set_pick(int lvl, int j) { chosen[lvl - base] = uint8_t(j); }
+};
+
+// ---------------------------------------------------------- DFS core -----
+//
+// Lockstep form: in every round each busy lane evaluates exactly one node
+// (one gaps() call), so a warp's lanes run the expensive walk together no
+// matter where each is in its own tree.  Between evaluations a lane
+// `advance`s: it backtracks over exhausted levels and inserts its next
+// untried item, which names the level to evaluate next.
+
+// Position the lane on its next node.  Items root..lvl-1 are inserted and
+// S[lvl] holds lvl's untried positions.  Backtracks over exhausted levels,
+// inserts item lvl after the next untried position and returns lvl + 1 (the
+// level to evaluate), or -1 when the unit's subtree is exhausted.
+template <class Stk, int TPB>
+__device__ __forceinline__ int advance(const List<TPB> &L, Stk &S, int &lvl, int root) {
     for (;;) {
-        const uint64_t cur = S.mask[lvl];
+        const uint64_t cur = S.get(lvl);
         if (cur == 0) {
-            if (lvl == root) return true;
+            if (lvl == root) return -1;
             --lvl;
-            L.put(S.chosen[lvl], L.get(lvl));  // detach item lvl
+            L.put(S.pick(lvl), L.get(lvl));  // detach item lvl
             continue;
         }
-        if (budget == 0) return false;
-        --budget;
         const int j = __ffsll(static_cast<long long>(cur)) - 1;
-        S.mask[lvl] = cur & (cur - 1);
-        const int after = L.get(j);
-        L.put(lvl, after);  // insert item lvl after j
+        S.set(lvl, cur & (cur - 1));
+        L.put(lvl, L.get(j));  // insert item lvl after j
         L.put(j, lvl);
-        const int nxt = lvl + 1;
-        const uint64_t g = R.gaps(L, nxt, nodes, bad);
-        if (bad) return true;
-        if (nxt == last) {
-            leaves += __popcll(g);
-            L.put(j, after);
-            continue;
-        }
-        S.chosen[lvl] = static_cast<uint8_t>(j);
-        lvl = nxt;
-        S.mask[lvl] = g;
+        S.set_pick(lvl, j);
+        return lvl + 1;
     }
 }
 
-// Start a unit whose list is loaded: evaluate the root level.  Returns true
-// if the unit still needs a search (mask[root] set), false if it is already
-// counted into `leaves`.
-template <class Rules, int TPB>
-__device__ __forceinline__ bool dfs_begin(const Rules &R, const List<TPB> &L, Stack &S, int root,
-                                          int last, unsigned long long &leaves,
-                                          unsigned long long &nodes, bool &bad) {
-    if (root > last) {  // nothing left to place: the unit is one completion
-        leaves += 1;
-        return false;
-    }
-    const uint64_t g = R.gaps(L, root, nodes, bad);
-    if (bad) return false;
-    if (root == last) {
+// Consume the evaluation g of level `eval`.  The last level is never
+// entered: its positions are counted and the item above it detached again.
+// Returns true when a fresh unit turns out to be finished by this round.
+template <class Stk, int TPB>
+__device__ __forceinline__ bool apply(const List<TPB> &L, Stk &S, int &lvl, int eval, int root,
+                                      int last, bool fresh, uint64_t g,
+                                      unsigned long long &leaves) {
+    if (eval == last) {
         leaves += __popcll(g);
+        if (fresh) return true;
+        L.put(S.pick(lvl), L.get(lvl));  // detach item lvl (= eval - 1)
         return false;
     }
-    S.mask[root] = g;
-    return true;
+    lvl = eval;
+    S.set(lvl, g);
+    (void)root;
+    return false;
 }
 
 template <int TPB, int WORDS>
@@ -253,48 +269,115 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
     return v;
 }
 
-// ------------------------------------------------------- plain kernels ---
-
-struct EdgePages {
-    uint32_t w[64];  // 4 pages x 64 bytes
+// Shared-memory carve-up of one CTA: [tables][lists][mask stack][picks].
+template <int TPB, int WORDS, int LEVELS>
+struct Carve {
+    static constexpr size_t kList = size_t(WORDS) * 4 * TPB;
+    static constexpr size_t kMask = size_t(LEVELS) * 8 * TPB;
+    static constexpr size_t kPick = size_t((LEVELS + 3) / 4) * 4 * TPB;
+    static constexpr size_t kThreadBytes = kList + kMask + kPick;
+    __device__ static List<TPB> list(uint8_t *smem, size_t tables) {
+        return List<TPB>{smem + tables + 4 * threadIdx.x};
+    }
+    __device__ static SmemStack<TPB, LEVELS> stack(uint8_t *smem, size_t tables) {
+        SmemStack<TPB, LEVELS> s;
+        s.mask = reinterpret_cast<uint64_t *>(smem + tables + kList) + threadIdx.x;
+        s.chosen = List<TPB>{smem + tables + kList + kMask + 4 * threadIdx.x};
+        s.base = 0;
+        return s;
+    }
 };
 
+template <int TPB, int WORDS>
+struct Carve<TPB, WORDS, 0> {  // local-memory stack
+    static constexpr size_t kList = size_t(WORDS) * 4 * TPB;
+    static constexpr size_t kThreadBytes = kList;
+    __device__ static List<TPB> list(uint8_t *smem, size_t tables) {
+        return List<TPB>{smem + tables + 4 * threadIdx.x};
+    }
+};
+
+template <int TPB, int LEVELS>
+struct StackOf {
+    using type = SmemStack<TPB, LEVELS>;
+};
 template <int TPB>
+struct StackOf<TPB, 0> {
+    using type = LocalStack;
+};
+
+template <int TPB, int WORDS, int LEVELS>
+__device__ __forceinline__ void init_stack(SmemStack<TPB, LEVELS> &S, uint8_t *smem, size_t tables) {
+    S = Carve<TPB, WORDS, LEVELS>::stack(smem, tables);
+}
+template <int TPB, int WORDS, int LEVELS>
+__device__ __forceinline__ void init_stack(LocalStack &S, uint8_t *, size_t) {
+    S.base = 0;
+}
+
+// Run one loaded unit per lane to completion in lockstep rounds (no refill):
+// the plain one-thread-per-unit kernels.
+template <class Rules, class Stk, int TPB>
+__device__ __forceinline__ void run_units(const Rules &R, const List<TPB> &L, Stk &S, bool busy,
+                                          int root, int last, unsigned long long &leaves,
+                                          unsigned long long &nodes) {
+    int lvl = root, eval = root;
+    bool fresh = true;
+    if (busy && root > last) {  // nothing left to place: one completion
+        leaves += 1;
+        busy = false;
+    }
+    while (__any_sync(kFull, busy)) {
+        if (busy) {
+            const uint64_t g = R.gaps(L, eval, nodes);
+            if (apply(L, S, lvl, eval, root, last, fresh, g, leaves)) {
+                busy = false;
+            } else {
+                fresh = false;
+                eval = advance(L, S, lvl, root);
+                busy = eval >= 0;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------- plain kernels ---
+
+// One thread per case: d_counts[k] = completions of case k (UINT64_MAX if
+// its cycle is malformed).  Shared memory: 4 edge pages, then the carve.
+template <int TPB, int LEVELS>
 __global__ void __launch_bounds__(TPB)
-    sym_plain_kernel(EdgePages pages, int start_i, int stop_i, const uint8_t *__restrict__ cycles,
-                     uint64_t num, unsigned long long *__restrict__ counts,
+    sym_plain_kernel(const uint8_t *__restrict__ edges, int start_i, int stop_i,
+                     const uint8_t *__restrict__ cycles, uint64_t num,
+                     unsigned long long *__restrict__ counts,
                      unsigned long long *__restrict__ nodes_out) {
-    __shared__ uint32_t s_edge[64];
-    __shared__ uint32_t s_list[16 * TPB];
-    const int tid = threadIdx.x;
-    for (int k = tid; k < 64; k += TPB) s_edge[k] = pages.w[k];
-    const List<TPB> L{reinterpret_cast<uint8_t *>(s_list) + 4 * tid};
-    const uint64_t unit = uint64_t(blockIdx.x) * TPB + tid;
+    extern __shared__ __align__(16) uint8_t smem[];
+    constexpr size_t kTables = 4 * kSymCells;
+    using C = Carve<TPB, 16, LEVELS>;
+    for (int k = threadIdx.x; k < 64; k += TPB)
+        reinterpret_cast<uint32_t *>(smem)[k] = __ldg(reinterpret_cast<const uint32_t *>(edges) + k);
+    const List<TPB> L = C::list(smem, kTables);
+    typename StackOf<TPB, LEVELS>::type S;
+    init_stack<TPB, 16, LEVELS>(S, smem, kTables);
+    const uint64_t unit = uint64_t(blockIdx.x) * TPB + threadIdx.x;
     const bool active = unit < num;
     if (active) load_list<TPB, 16>(L, cycles + unit * kSymCells, kSymCells);
     __syncthreads();
 
-    unsigned long long nodes = 0;
-    if (active) {
-        const SymRules R{reinterpret_cast<const uint8_t *>(s_edge)};
-        Stack S;
-        bool bad = !list_valid(L, start_i);
-        unsigned long long leaves = 0;
-        const int last = stop_i - 1;
-        if (!bad && dfs_begin(R, L, S, start_i, last, leaves, nodes, bad)) {
-            int lvl = start_i;
-            while (!dfs_run(R, L, S, lvl, start_i, last, leaves, nodes, 0xffffffffu, bad)) {
-            }
-        }
-        counts[unit] = bad ? ~0ULL : leaves;
-    }
+    unsigned long long nodes = 0, leaves = 0;
+    const bool bad = active && !list_valid(L, start_i);
+    S.base = start_i;
+    run_units(SymRules{smem}, L, S, active && !bad, start_i, stop_i - 1, leaves, nodes);
+    if (active) counts[unit] = bad ? ~0ULL : leaves;
     if (nodes_out) {
         const unsigned long long s = warp_sum(nodes);
-        if ((tid & 31) == 0 && s) atomicAdd(nodes_out, s);
+        if ((threadIdx.x & 31) == 0 && s) atomicAdd(nodes_out, s);
     }
 }
 
-template <int TPB>
+// One thread per prefix state.  Shared memory: the map's neighbour table,
+// then the carve.
+template <int TPB, int LEVELS>
 __global__ void __launch_bounds__(TPB)
     lunnon_plain_kernel(const uint8_t *__restrict__ table, int table_bytes, int n, int dim,
                         int start_leaf, const uint8_t *__restrict__ states, uint32_t stride,
@@ -302,154 +385,114 @@ __global__ void __launch_bounds__(TPB)
                         unsigned long long *__restrict__ total,
                         unsigned long long *__restrict__ nodes_out) {
     extern __shared__ __align__(16) uint8_t smem[];
-    uint32_t *s_list = reinterpret_cast<uint32_t *>(smem);  // 17 * TPB words
-    uint8_t *s_table = smem + 17 * 4 * TPB;
-    const int tid = threadIdx.x;
-    for (int k = tid; k < table_bytes / 4; k += TPB)
-        reinterpret_cast<uint32_t *>(s_table)[k] = __ldg(reinterpret_cast<const uint32_t *>(table) + k);
-    const List<TPB> L{reinterpret_cast<uint8_t *>(s_list) + 4 * tid};
-    const uint64_t unit = uint64_t(blockIdx.x) * TPB + tid;
+    using C = Carve<TPB, 17, LEVELS>;
+    for (int k = threadIdx.x; k < table_bytes / 4; k += TPB)
+        reinterpret_cast<uint32_t *>(smem)[k] = __ldg(reinterpret_cast<const uint32_t *>(table) + k);
+    const List<TPB> L = C::list(smem, table_bytes);
+    typename StackOf<TPB, LEVELS>::type S;
+    init_stack<TPB, 17, LEVELS>(S, smem, table_bytes);
+    const uint64_t unit = uint64_t(blockIdx.x) * TPB + threadIdx.x;
     const bool active = unit < num;
     if (active) load_list<TPB, 17>(L, states + unit * stride, stride);
     __syncthreads();
 
-    unsigned long long nodes = 0;
-    unsigned long long leaves = 0;
-    if (active) {
-        const LunnonRules R{s_table, n, dim};
-        Stack S;
-        bool bad = !list_valid(L, start_leaf < n + 1 ? start_leaf : n + 1);
-        if (!bad && dfs_begin(R, L, S, start_leaf, n, leaves, nodes, bad)) {
-            int lvl = start_leaf;
-            while (!dfs_run(R, L, S, lvl, start_leaf, n, leaves, nodes, 0xffffffffu, bad)) {
-            }
-        }
-        leaves = bad ? 0 : leaves * static_cast<unsigned long long>(n);
-        if (per_state) per_state[unit] = bad ? ~0ULL : leaves;
-    }
+    unsigned long long nodes = 0, leaves = 0;
+    const bool bad = active && !list_valid(L, start_leaf < n + 1 ? start_leaf : n + 1);
+    S.base = start_leaf;
+    run_units(LunnonRules{smem, n, dim}, L, S, active && !bad, start_leaf, n, leaves, nodes);
+    leaves = bad ? 0 : leaves * static_cast<unsigned long long>(n);
+    if (active && per_state) per_state[unit] = bad ? ~0ULL : leaves;
     if (total) {
         const unsigned long long s = warp_sum(leaves);
-        if ((tid & 31) == 0 && s) atomicAdd(total, s);
+        if ((threadIdx.x & 31) == 0 && s) atomicAdd(total, s);
     }
     if (nodes_out) {
         const unsigned long long s = warp_sum(nodes);
-        if ((tid & 31) == 0 && s) atomicAdd(nodes_out, s);
+        if ((threadIdx.x & 31) == 0 && s) atomicAdd(nodes_out, s);
     }
 }
 
 // ------------------------------------------------- persistent kernels ----
 
+// Bounded multi-producer multi-consumer ring of split items (the sequence-
+// numbered cell scheme of D. Vyukov's bounded MPMC queue): cell c holds
+// seq == ticket when free for the producer of `ticket`, ticket + 1 once that
+// producer has published it, and ticket + capacity once its consumer has
+// copied it out.  Producers and consumers only ever claim a cell whose
+// sequence already says it is ready for them, so nobody waits on anybody.
 struct Queue {
     QueueHeader *hdr;
     TaskRecord *slots;
-    unsigned int *ready;
-    unsigned long long capacity;
+    unsigned long long *seq;
+    unsigned long long capacity;  // power of two
 };
 
 __device__ __forceinline__ unsigned long long vload(const unsigned long long *p) {
     return *reinterpret_cast<const volatile unsigned long long *>(p);
 }
 
-// Hand out one work item: an initial unit while any are left (an atomicAdd
-// that may overshoot harmlessly), otherwise a split subtree (a CAS that never
-// hands out an index that has not been reserved).  Returns 0 = none,
-// 1 = initial unit k, 2 = split item k.
-__device__ __forceinline__ int take_item(const Queue &Q, unsigned long long num,
-                                         unsigned long long &k) {
-    if (vload(&Q.hdr->init_next) < num) {
-        k = atomicAdd(&Q.hdr->init_next, 1ULL);
-        if (k < num) return 1;
-    }
-    unsigned long long h = vload(&Q.hdr->spawn_head);
-    for (int attempt = 0; attempt < 32; ++attempt) {
-        const unsigned long long t = vload(&Q.hdr->spawn_tail);
-        if (h >= t) return 0;
-        const unsigned long long seen = atomicCAS(&Q.hdr->spawn_head, h, h + 1);
-        if (seen == h) {
-            k = h;
-            return 2;
+__device__ __forceinline__ bool ring_push(const Queue &Q, const uint32_t (&w)[24]) {
+    unsigned long long pos = vload(&Q.hdr->spawn_tail);
+    for (int attempt = 0; attempt < 64; ++attempt) {
+        const unsigned long long cell = pos & (Q.capacity - 1);
+        const long long diff = (long long)(vload(Q.seq + cell) - pos);
+        if (diff == 0) {
+            const unsigned long long seen = atomicCAS(&Q.hdr->spawn_tail, pos, pos + 1);
+            if (seen == pos) {
+                uint4 *dst = reinterpret_cast<uint4 *>(Q.slots + cell);
+#pragma unroll
+                for (int q = 0; q < 6; ++q)
+                    __stcg(dst + q, make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]));
+                __threadfence();
+                atomicExch(Q.seq + cell, pos + 1);
+                return true;
+            }
+            pos = seen;
+        } else if (diff < 0) {
+            return false;  // full
+        } else {
+            pos = vload(&Q.hdr->spawn_tail);
         }
-        h = seen;
     }
-    return 0;
+    return false;
 }
 
-// Wait (bounded) until split item k is published, then copy it out.
-template <int TPB, int WORDS>
-__device__ __forceinline__ bool fetch_split(const Queue &Q, unsigned long long k, const List<TPB> &L,
-                                            uint32_t &owner, uint64_t &mask, int &level,
-                                            uint32_t wait_limit) {
-    const volatile unsigned int *flag = Q.ready + k;
-    uint32_t spins = 0;
-    while (*flag == 0u) {
-        if (++spins > wait_limit) {
-            atomicExch(&Q.hdr->error, 1u);
-            return false;
+__device__ __forceinline__ bool ring_pop(const Queue &Q, uint32_t (&w)[24]) {
+    unsigned long long pos = vload(&Q.hdr->spawn_head);
+    for (int attempt = 0; attempt < 64; ++attempt) {
+        const unsigned long long cell = pos & (Q.capacity - 1);
+        const long long diff = (long long)(vload(Q.seq + cell) - (pos + 1));
+        if (diff == 0) {
+            const unsigned long long seen = atomicCAS(&Q.hdr->spawn_head, pos, pos + 1);
+            if (seen == pos) {
+                __threadfence();
+                const uint4 *src = reinterpret_cast<const uint4 *>(Q.slots + cell);
+#pragma unroll
+                for (int q = 0; q < 6; ++q) {
+                    const uint4 x = __ldcg(src + q);
+                    w[4 * q] = x.x;
+                    w[4 * q + 1] = x.y;
+                    w[4 * q + 2] = x.z;
+                    w[4 * q + 3] = x.w;
+                }
+                __threadfence();
+                atomicExch(Q.seq + cell, pos + Q.capacity);
+                return true;
+            }
+            pos = seen;
+        } else if (diff < 0) {
+            return false;  // empty
+        } else {
+            pos = vload(&Q.hdr->spawn_head);
         }
-        __nanosleep(64);
     }
-    __threadfence();
-    const uint4 *src = reinterpret_cast<const uint4 *>(Q.slots + k);
-    uint32_t w[24];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        const uint4 x = __ldcg(src + q);
-        w[4 * q] = x.x;
-        w[4 * q + 1] = x.y;
-        w[4 * q + 2] = x.z;
-        w[4 * q + 3] = x.w;
-    }
-#pragma unroll
-    for (int k2 = 0; k2 < WORDS; ++k2) L.set_word(k2, w[k2]);
-    owner = w[17];
-    mask = uint64_t(w[18]) | (uint64_t(w[19]) << 32);
-    level = int(w[20]);
-    return true;
+    return false;
 }
 
-// Give away the shallowest untried sibling set of this unit as a new work
-// item.  The list is rolled back to that level, copied, and replayed.
-template <int TPB, int WORDS>
-__device__ __forceinline__ bool donate(const Queue &Q, const List<TPB> &L, Stack &S, int lvl,
-                                       int root, int last, uint32_t owner) {
-    int s = root;
-    while (s <= lvl && S.mask[s] == 0) ++s;
-    if (s > lvl || last - s < kMinSplitHeight) return false;
-    // Reserve a slot without ever overshooting the capacity.
-    unsigned long long t = vload(&Q.hdr->spawn_tail);
-    bool got = false;
-    for (int attempt = 0; attempt < 32 && t < Q.capacity; ++attempt) {
-        const unsigned long long seen = atomicCAS(&Q.hdr->spawn_tail, t, t + 1);
-        if (seen == t) {
-            got = true;
-            break;
-        }
-        t = seen;
-    }
-    if (!got) return false;
-    for (int l = lvl - 1; l >= s; --l) L.put(S.chosen[l], L.get(l));
-    uint32_t w[24];
-#pragma unroll
-    for (int k = 0; k < 24; ++k) w[k] = 0;
-#pragma unroll
-    for (int k = 0; k < WORDS; ++k) w[k] = L.word(k);
-    w[17] = owner;
-    w[18] = uint32_t(S.mask[s]);
-    w[19] = uint32_t(S.mask[s] >> 32);
-    w[20] = uint32_t(s);
-    uint4 *dst = reinterpret_cast<uint4 *>(Q.slots + t);
-#pragma unroll
-    for (int q = 0; q < 6; ++q) __stcg(dst + q, make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]));
-    for (int l = s; l < lvl; ++l) {
-        const int j = S.chosen[l];
-        const int after = L.get(j);
-        L.put(l, after);
-        L.put(j, l);
-    }
-    S.mask[s] = 0;
-    __threadfence();
-    atomicExch(Q.ready + t, 1u);
-    return true;
+__global__ void ring_init_kernel(unsigned long long *seq, unsigned long long capacity) {
+    for (unsigned long long k = blockIdx.x * blockDim.x + threadIdx.x; k < capacity;
+         k += gridDim.x * blockDim.x)
+        seq[k] = k;
 }
 
 struct SymSource {
@@ -462,41 +505,39 @@ struct LunnonSource {
     const uint8_t *states;
     const uint32_t *state_owner;
     const LunnonInstanceDev *inst;
-    const uint8_t *tables;
     uint32_t stride;
 };
 
-// The persistent loop.  Every lane holds at most one unit; lanes that run out
-// of work refill individually inside their slice, and at the slice boundary
-// the warp (re)converges to refill, check whether the queue is running dry
-// and, if so, let each busy lane give away its shallowest untried siblings.
-// A warp leaves when it is idle and all work is accounted for, or when it has
-// stayed idle for wait_limit rounds -- leaving is always safe, because the
-// warp that owns a split item's parent keeps looping until it has nothing.
-template <int TPB, int WORDS, bool kSym>
+// The persistent loop, in lockstep rounds.  Each round: idle lanes refill
+// (initial units through one warp-aggregated atomicAdd, then split items),
+// every busy lane evaluates one node, consumes it and advances to its next
+// node.  Every `period` rounds the warp accounts finished units and, once
+// the initial units are handed out and the queue is running dry, lets each
+// busy lane give away its shallowest untried siblings.  A warp leaves when it
+// is idle and all work is accounted for, or when it has stayed idle for
+// wait_limit rounds -- leaving is always safe, because the warp that owns a
+// split item's parent keeps looping until it has nothing left.
+template <int TPB, int WORDS, bool kSym, class Stk>
 __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables, const SymSource &sym,
                                                 const LunnonSource &lun, unsigned long long num,
                                                 unsigned long long *counts,
                                                 unsigned long long *nodes_out, const Queue &Q,
-                                                uint32_t budget, unsigned long long hungry_level,
-                                                uint32_t wait_limit, const List<TPB> &L) {
+                                                uint32_t period, unsigned long long hungry_level,
+                                                uint32_t wait_limit, const List<TPB> &L, Stk &S) {
     const int lane = threadIdx.x & 31;
-    Stack S;
-    bool busy = false;
-    bool bad = false;
-    int lvl = 0, root = 0, last = 0;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    bool busy = false, fresh = false;
+    int lvl = 0, root = 0, last = 0, eval = 0;
     uint32_t owner = 0;
     unsigned long long leaves = 0, nodes = 0, finished = 0, started = 0;
-    uint32_t idle_rounds = 0;
-    SymRules srules{s_tables};
-    LunnonRules lrules{nullptr, 0, 0};
+    uint32_t idle_rounds = 0, round = 0;
+    bool tail_phase = false;  // all initial units handed out
+    const SymRules srules{s_tables};
+    LunnonRules lrules{s_tables, 0, 0};
 
     // Count a finished unit into its owner's slot.
     auto flush = [&]() {
-        if (bad) {
-            atomicExch(&Q.hdr->error, 1u);
-            bad = false;
-        } else if (leaves) {
+        if (leaves) {
             const unsigned long long weight = kSym ? 1ULL : static_cast<unsigned long long>(lrules.n);
             atomicAdd(counts + owner, leaves * weight);
         }
@@ -504,68 +545,115 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables, const S
         ++finished;
     };
 
-    // Acquire work until a unit needs a search or nothing is available.
-    auto acquire = [&]() -> bool {
-        for (int tries = 0; tries < 64; ++tries) {
-            unsigned long long k = 0;
-            const int kind = take_item(Q, num, k);
-            if (kind == 0) return false;
-            ++started;
-            if (kind == 1) {
-                if (kSym) {
-                    load_list<TPB, WORDS>(L, sym.cycles + k * kSymCells, kSymCells);
-                    owner = uint32_t(k);
-                    root = sym.start_i;
-                    last = sym.last;
-                    bad = !list_valid(L, root);
-                } else {
-                    load_list<TPB, WORDS>(L, lun.states + k * lun.stride, lun.stride);
-                    owner = lun.state_owner[k];
-                    const LunnonInstanceDev I = lun.inst[owner];
-                    lrules = LunnonRules{s_tables + I.table_offset, I.n, I.dim};
-                    root = I.start_leaf;
-                    last = I.n;
-                    bad = !list_valid(L, root < I.n + 1 ? root : I.n + 1);
-                }
-                if (bad) {
-                    flush();
-                    continue;
-                }
-                bool more;
-                if (kSym) more = dfs_begin(srules, L, S, root, last, leaves, nodes, bad);
-                else more = dfs_begin(lrules, L, S, root, last, leaves, nodes, bad);
-                if (more && !bad) {
-                    lvl = root;
-                    return true;
-                }
-                flush();
-            } else {
-                uint64_t mask = 0;
-                int level = 0;
-                if (!fetch_split<TPB, WORDS>(Q, k, L, owner, mask, level, wait_limit)) {
-                    ++finished;
-                    continue;
-                }
-                if (kSym) {
-                    last = sym.last;
-                } else {
-                    const LunnonInstanceDev I = lun.inst[owner];
-                    lrules = LunnonRules{s_tables + I.table_offset, I.n, I.dim};
-                    last = I.n;
-                }
-                root = level;
-                lvl = level;
-                S.mask[level] = mask;
-                return true;
-            }
+    auto set_instance = [&](uint32_t inst) {
+        const LunnonInstanceDev I = lun.inst[inst];
+        lrules = LunnonRules{s_tables + I.table_offset, I.n, I.dim};
+        last = I.n;
+        S.base = I.start_leaf;
+        return I;
+    };
+
+    // Load initial unit k; returns true if it needs a search.
+    auto load_initial = [&](unsigned long long k) -> bool {
+        ++started;
+        bool bad;
+        if (kSym) {
+            load_list<TPB, WORDS>(L, sym.cycles + k * kSymCells, kSymCells);
+            owner = uint32_t(k);
+            root = sym.start_i;
+            last = sym.last;
+            S.base = root;
+            bad = !list_valid(L, root);
+        } else {
+            load_list<TPB, WORDS>(L, lun.states + k * lun.stride, lun.stride);
+            owner = lun.state_owner[k];
+            const LunnonInstanceDev I = set_instance(owner);
+            root = I.start_leaf;
+            bad = !list_valid(L, root < I.n + 1 ? root : I.n + 1);
         }
-        return false;
+        if (bad) {
+            atomicExch(&Q.hdr->error, 1u);
+            ++finished;
+            return false;
+        }
+        if (root > last) {  // nothing left to place: one completion
+            leaves = 1;
+            flush();
+            return false;
+        }
+        lvl = root;
+        eval = root;
+        fresh = true;
+        return true;
+    };
+
+    // Load a split item; returns true if one was available.
+    auto load_split = [&]() -> bool {
+        uint32_t w[24];
+        if (!ring_pop(Q, w)) return false;
+        ++started;
+#pragma unroll
+        for (int k2 = 0; k2 < WORDS; ++k2) L.set_word(k2, w[k2]);
+        owner = w[17];
+        root = int(w[20]);
+        if (kSym) {
+            last = sym.last;
+            S.base = sym.start_i;
+        } else {
+            set_instance(owner);
+        }
+        lvl = root;
+        S.set(root, uint64_t(w[18]) | (uint64_t(w[19]) << 32));
+        eval = advance(L, S, lvl, root);  // the item's mask is never empty
+        fresh = false;
+        return eval >= 0;
+    };
+
+    // Give away the shallowest untried sibling set as a split item.  Items
+    // root..lvl are inserted (lvl's evaluation is pending): roll the list back
+    // to that level, copy it out, replay.
+    auto donate = [&]() {
+        int s = root;
+        while (s < lvl && S.get(s) == 0) ++s;
+        const uint64_t m = S.get(s);
+        if (m == 0 || last - s < kMinSplitHeight) return;
+        for (int l = lvl; l >= s; --l) L.put(S.pick(l), L.get(l));
+        uint32_t w[24];
+#pragma unroll
+        for (int k = 0; k < 24; ++k) w[k] = 0;
+#pragma unroll
+        for (int k = 0; k < WORDS; ++k) w[k] = L.word(k);
+        w[17] = owner;
+        w[18] = uint32_t(m);
+        w[19] = uint32_t(m >> 32);
+        w[20] = uint32_t(s);
+        for (int l = s; l <= lvl; ++l) {
+            const int j = S.pick(l);
+            L.put(l, L.get(j));
+            L.put(j, l);
+        }
+        if (ring_push(Q, w)) S.set(s, 0);
     };
 
     for (;;) {
-        if (!busy) busy = acquire();
-        const unsigned any = __ballot_sync(kFull, busy);
-        if (any == 0) {
+        // Refill idle lanes: initial units first, one atomic per warp.
+        const unsigned need = __ballot_sync(kFull, !busy);
+        if (need) {
+            unsigned long long base = num;
+            const int leader = __ffs(need) - 1;
+            if (!tail_phase && lane == leader) {
+                if (vload(&Q.hdr->init_next) < num)
+                    base = atomicAdd(&Q.hdr->init_next, (unsigned long long)__popc(need));
+            }
+            base = __shfl_sync(kFull, base, leader);
+            if (base >= num) tail_phase = true;
+            if (!busy) {
+                const unsigned long long k = base + __popc(need & lt_mask);
+                if (k < num) busy = load_initial(k);
+                else if (tail_phase) busy = load_split();
+            }
+        }
+        if (!__any_sync(kFull, busy)) {
             // Account this warp's finished units first, then decide.
             const unsigned long long f = warp_sum(finished);
             finished = 0;
@@ -579,39 +667,45 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables, const S
             }
             stop = __shfl_sync(kFull, stop, 0);
             if (stop) break;
-            __nanosleep(200);
+            __nanosleep(256);
             continue;
         }
         idle_rounds = 0;
+        // One evaluation per busy lane.
         if (busy) {
-            // Run the slice; a lane whose unit ends refills and keeps going.
-            uint32_t left = budget;
-            for (;;) {
-                bool done;
-                if (kSym) done = dfs_run(srules, L, S, lvl, root, last, leaves, nodes, left, bad);
-                else done = dfs_run(lrules, L, S, lvl, root, last, leaves, nodes, left, bad);
-                if (!done) break;
+            uint64_t g;
+            if (kSym) g = srules.gaps(L, eval, nodes);
+            else g = lrules.gaps(L, eval, nodes);
+            bool done = apply(L, S, lvl, eval, root, last, fresh, g, leaves);
+            if (!done) {
+                fresh = false;
+                eval = advance(L, S, lvl, root);
+                done = eval < 0;
+            }
+            if (done) {
                 flush();
-                busy = acquire();
-                if (!busy) break;
-                left = budget / 2;  // a fresh unit gets a shorter remaining slice
+                busy = false;
             }
         }
-        // Slice boundary: account finished units, then split if the queue is
-        // running dry.
-        const unsigned long long f = warp_sum(finished);
-        int hungry = 0;
-        if (lane == 0) {
-            if (f) atomicAdd(&Q.hdr->completed, f);
-            const unsigned long long in = vload(&Q.hdr->init_next);
-            const unsigned long long init_left = in < num ? num - in : 0;
-            const unsigned long long split_left =
-                vload(&Q.hdr->spawn_tail) - vload(&Q.hdr->spawn_head);
-            hungry = (init_left + split_left) < hungry_level;
+        // Bookkeeping every `period` rounds.
+        if (++round >= period) {
+            round = 0;
+            const unsigned long long f = warp_sum(finished);
+            finished = 0;
+            int hungry = 0, tail = tail_phase;
+            if (lane == 0) {
+                if (f) atomicAdd(&Q.hdr->completed, f);
+                if (!tail) tail = vload(&Q.hdr->init_next) >= num;
+                if (tail) {
+                    const unsigned long long queued =
+                        vload(&Q.hdr->spawn_tail) - vload(&Q.hdr->spawn_head);
+                    hungry = queued < hungry_level;
+                }
+            }
+            tail_phase = __shfl_sync(kFull, tail, 0) != 0;
+            hungry = __shfl_sync(kFull, hungry, 0);
+            if (hungry && busy && !fresh) donate();
         }
-        finished = 0;
-        hungry = __shfl_sync(kFull, hungry, 0);
-        if (hungry && busy) donate<TPB, WORDS>(Q, L, S, lvl, root, last, owner);
     }
 
     const unsigned long long ns = warp_sum(nodes);
@@ -622,37 +716,75 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables, const S
     }
 }
 
-template <int TPB>
+template <int TPB, int LEVELS>
 __global__ void __launch_bounds__(TPB)
-    sym_batched_kernel(EdgePages pages, SymSource src, unsigned long long num,
+    sym_batched_kernel(const uint8_t *__restrict__ edges, SymSource src, unsigned long long num,
                        unsigned long long *counts, unsigned long long *nodes_out, Queue Q,
-                       uint32_t budget, unsigned long long hungry_level, uint32_t wait_limit) {
-    __shared__ uint32_t s_edge[64];
-    __shared__ uint32_t s_list[16 * TPB];
-    for (int k = threadIdx.x; k < 64; k += TPB) s_edge[k] = pages.w[k];
+                       uint32_t period, unsigned long long hungry_level, uint32_t wait_limit) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    constexpr size_t kTables = 4 * kSymCells;
+    using C = Carve<TPB, 16, LEVELS>;
+    for (int k = threadIdx.x; k < 64; k += TPB)
+        reinterpret_cast<uint32_t *>(smem)[k] = __ldg(reinterpret_cast<const uint32_t *>(edges) + k);
     __syncthreads();
-    const List<TPB> L{reinterpret_cast<uint8_t *>(s_list) + 4 * threadIdx.x};
+    const List<TPB> L = C::list(smem, kTables);
+    typename StackOf<TPB, LEVELS>::type S;
+    init_stack<TPB, 16, LEVELS>(S, smem, kTables);
     LunnonSource none{};
-    persistent_loop<TPB, 16, true>(reinterpret_cast<const uint8_t *>(s_edge), src, none, num, counts,
-                                   nodes_out, Q, budget, hungry_level, wait_limit, L);
+    persistent_loop<TPB, 16, true>(smem, src, none, num, counts, nodes_out, Q, period,
+                                   hungry_level, wait_limit, L, S);
 }
 
-template <int TPB>
+template <int TPB, int LEVELS>
 __global__ void __launch_bounds__(TPB)
-    lunnon_batched_kernel(LunnonSource src, uint32_t tables_bytes, unsigned long long num,
-                          unsigned long long *counts, unsigned long long *nodes_out, Queue Q,
-                          uint32_t budget, unsigned long long hungry_level, uint32_t wait_limit) {
+    lunnon_batched_kernel(const uint8_t *__restrict__ tables, uint32_t tables_bytes,
+                          LunnonSource src, unsigned long long num, unsigned long long *counts,
+                          unsigned long long *nodes_out, Queue Q, uint32_t period,
+                          unsigned long long hungry_level, uint32_t wait_limit) {
     extern __shared__ __align__(16) uint8_t smem[];
-    uint32_t *s_list = reinterpret_cast<uint32_t *>(smem);
-    uint8_t *s_tables = smem + 17 * 4 * TPB;
+    using C = Carve<TPB, 17, LEVELS>;
     for (uint32_t k = threadIdx.x; k < tables_bytes / 4; k += TPB)
-        reinterpret_cast<uint32_t *>(s_tables)[k] =
-            __ldg(reinterpret_cast<const uint32_t *>(src.tables) + k);
+        reinterpret_cast<uint32_t *>(smem)[k] = __ldg(reinterpret_cast<const uint32_t *>(tables) + k);
     __syncthreads();
-    const List<TPB> L{reinterpret_cast<uint8_t *>(s_list) + 4 * threadIdx.x};
+    const List<TPB> L = C::list(smem, tables_bytes);
+    typename StackOf<TPB, LEVELS>::type S;
+    init_stack<TPB, 17, LEVELS>(S, smem, tables_bytes);
     SymSource none{};
-    persistent_loop<TPB, 17, false>(s_tables, none, src, num, counts, nodes_out, Q, budget,
-                                    hungry_level, wait_limit, L);
+    persistent_loop<TPB, 17, false>(smem, none, src, num, counts, nodes_out, Q, period,
+                                    hungry_level, wait_limit, L, S);
+}
+
+// ------------------------------------------------------- launch helpers --
+
+// MF_STACK_MODE=local forces the local-memory stack (a tuning aid).
+bool env_local_stack() {
+    static const bool local = [] {
+        const char *e = std::getenv("MF_STACK_MODE");
+        return e && std::strcmp(e, "local") == 0;
+    }();
+    return local;
+}
+
+// Smallest compiled stack depth that holds `levels` levels (0 = local).
+int pick_levels(int levels, bool local = false) {
+    if (local || env_local_stack()) return 0;
+    if (levels <= 24) return 24;
+    if (levels <= 32) return 32;
+    if (levels <= 48) return 48;
+    return 0;
+}
+
+template <class K>
+cudaError_t prepare(K kernel, size_t smem, int tpb, int want_per_sm, int &blocks_per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(smem));
+    if (e != cudaSuccess) return e;
+    int fit = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kernel, tpb, smem);
+    if (e != cudaSuccess) return e;
+    if (fit < 1) return cudaErrorInvalidConfiguration;
+    blocks_per_sm = want_per_sm > 0 && want_per_sm < fit ? want_per_sm : fit;
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -667,9 +799,7 @@ int device_sm_count() {
 }
 
 uint64_t workspace_bytes(uint64_t capacity) {
-    const uint64_t slots = capacity * sizeof(TaskRecord);
-    const uint64_t flags = (capacity * sizeof(unsigned int) + 255) / 256 * 256;
-    return 256 + slots + flags;
+    return 256 + capacity * sizeof(TaskRecord) + capacity * sizeof(unsigned long long);
 }
 
 namespace {
@@ -679,31 +809,46 @@ Queue carve_queue(void *ws, uint64_t capacity) {
     Queue q;
     q.hdr = reinterpret_cast<QueueHeader *>(p);
     q.slots = reinterpret_cast<TaskRecord *>(p + 256);
-    q.ready = reinterpret_cast<unsigned int *>(p + 256 + capacity * sizeof(TaskRecord));
+    q.seq = reinterpret_cast<unsigned long long *>(p + 256 + capacity * sizeof(TaskRecord));
     q.capacity = capacity;
     return q;
 }
 
-EdgePages pack_pages(const uint8_t *edges) {
-    EdgePages e;
-    for (int k = 0; k < 64; ++k)
-        e.w[k] = uint32_t(edges[4 * k]) | (uint32_t(edges[4 * k + 1]) << 8) |
-                 (uint32_t(edges[4 * k + 2]) << 16) | (uint32_t(edges[4 * k + 3]) << 24);
-    return e;
+cudaError_t reset_queue(const Queue &Q, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(Q.hdr, 0, 256, stream);
+    if (e != cudaSuccess) return e;
+    ring_init_kernel<<<64, 256, 0, stream>>>(Q.seq, Q.capacity);
+    return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t launch_sym_plain(const uint8_t *edges, int start_i, int stop_i, const uint8_t *d_cycles,
-                             uint64_t num, uint64_t *d_counts, uint64_t *d_nodes,
-                             cudaStream_t stream) {
+cudaError_t launch_sym_plain(const uint8_t *d_edges, int start_i, int stop_i,
+                             const uint8_t *d_cycles, uint64_t num, uint64_t *d_counts,
+                             uint64_t *d_nodes, cudaStream_t stream) {
     if (num == 0) return cudaSuccess;
     constexpr int TPB = 128;
     const uint64_t blocks = (num + TPB - 1) / TPB;
-    sym_plain_kernel<TPB><<<unsigned(blocks), TPB, 0, stream>>>(
-        pack_pages(edges), start_i, stop_i, d_cycles, num,
-        reinterpret_cast<unsigned long long *>(d_counts),
-        reinterpret_cast<unsigned long long *>(d_nodes));
+    const int levels = pick_levels(stop_i - 1 - start_i);
+    const size_t tables = 4 * kSymCells;
+    auto *counts = reinterpret_cast<unsigned long long *>(d_counts);
+    auto *nodes = reinterpret_cast<unsigned long long *>(d_nodes);
+    int bpsm = 0;
+#define MF_SYM_PLAIN(LV)                                                                        \
+    do {                                                                                        \
+        const size_t smem = tables + Carve<TPB, 16, LV>::kThreadBytes;                          \
+        cudaError_t e = prepare(sym_plain_kernel<TPB, LV>, smem, TPB, 0, bpsm);                 \
+        if (e != cudaSuccess) return e;                                                         \
+        sym_plain_kernel<TPB, LV><<<unsigned(blocks), TPB, smem, stream>>>(                     \
+            d_edges, start_i, stop_i, d_cycles, num, counts, nodes);                            \
+    } while (0)
+    switch (levels) {
+        case 24: MF_SYM_PLAIN(24); break;
+        case 32: MF_SYM_PLAIN(32); break;
+        case 48: MF_SYM_PLAIN(48); break;
+        default: MF_SYM_PLAIN(0); break;
+    }
+#undef MF_SYM_PLAIN
     return cudaGetLastError();
 }
 
@@ -714,83 +859,119 @@ cudaError_t launch_lunnon_plain(const uint8_t *d_table, int n, int dim, int star
     if (num == 0) return cudaSuccess;
     constexpr int TPB = 128;
     const int table_bytes = (dim * (n + 1) * (n + 1) + 15) / 16 * 16;
-    const size_t smem = size_t(17) * 4 * TPB + table_bytes;
-    cudaError_t e = cudaFuncSetAttribute(lunnon_plain_kernel<TPB>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    if (e != cudaSuccess) return e;
+    const int levels = pick_levels(n - start_leaf);
     const uint64_t blocks = (num + TPB - 1) / TPB;
-    lunnon_plain_kernel<TPB><<<unsigned(blocks), TPB, smem, stream>>>(
-        d_table, table_bytes, n, dim, start_leaf, d_states, stride, num,
-        reinterpret_cast<unsigned long long *>(d_per_state),
-        reinterpret_cast<unsigned long long *>(d_total),
-        reinterpret_cast<unsigned long long *>(d_nodes));
+    auto *per = reinterpret_cast<unsigned long long *>(d_per_state);
+    auto *tot = reinterpret_cast<unsigned long long *>(d_total);
+    auto *nodes = reinterpret_cast<unsigned long long *>(d_nodes);
+    int bpsm = 0;
+#define MF_LUN_PLAIN(LV)                                                                        \
+    do {                                                                                        \
+        const size_t smem = table_bytes + Carve<TPB, 17, LV>::kThreadBytes;                     \
+        cudaError_t e = prepare(lunnon_plain_kernel<TPB, LV>, smem, TPB, 0, bpsm);              \
+        if (e != cudaSuccess) return e;                                                         \
+        lunnon_plain_kernel<TPB, LV><<<unsigned(blocks), TPB, smem, stream>>>(                  \
+            d_table, table_bytes, n, dim, start_leaf, d_states, stride, num, per, tot, nodes);   \
+    } while (0)
+    switch (levels) {
+        case 24: MF_LUN_PLAIN(24); break;
+        case 32: MF_LUN_PLAIN(32); break;
+        case 48: MF_LUN_PLAIN(48); break;
+        default: MF_LUN_PLAIN(0); break;
+    }
+#undef MF_LUN_PLAIN
     return cudaGetLastError();
 }
 
-cudaError_t launch_sym_batched(const uint8_t *edges, int start_i, int stop_i,
+cudaError_t launch_sym_batched(const uint8_t *d_edges, int start_i, int stop_i,
                                const uint8_t *d_cycles, uint64_t num, uint64_t *d_counts,
                                uint64_t *d_nodes, void *d_workspace, const BatchKnobs &knobs,
                                cudaStream_t stream) {
     Queue Q = carve_queue(d_workspace, knobs.queue_capacity);
-    cudaError_t e = cudaMemsetAsync(d_workspace, 0, 256, stream);
-    if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(Q.ready, 0, knobs.queue_capacity * sizeof(unsigned int), stream);
+    cudaError_t e = reset_queue(Q, stream);
     if (e != cudaSuccess) return e;
     if (num == 0) return cudaSuccess;
     e = cudaMemsetAsync(d_counts, 0, num * sizeof(uint64_t), stream);
     if (e != cudaSuccess) return e;
     const int sms = device_sm_count();
-    SymSource src{d_cycles, start_i, stop_i - 1};
-    const unsigned long long threads = 1ULL * sms * knobs.blocks_per_sm * knobs.block_threads;
-    const unsigned long long hungry = threads * knobs.hungry_factor / 8;
-    const unsigned grid = unsigned(sms * knobs.blocks_per_sm);
-#define MF_SYM_BATCHED(TPB)                                                                      \
-    sym_batched_kernel<TPB><<<grid, TPB, 0, stream>>>(                                           \
-        pack_pages(edges), src, num, reinterpret_cast<unsigned long long *>(d_counts),           \
-        reinterpret_cast<unsigned long long *>(d_nodes), Q, knobs.node_budget, hungry,           \
-        knobs.wait_limit)
-    switch (knobs.block_threads) {
-        case 64: MF_SYM_BATCHED(64); break;
-        case 256: MF_SYM_BATCHED(256); break;
-        default: MF_SYM_BATCHED(128); break;
+    const SymSource src{d_cycles, start_i, stop_i - 1};
+    const int levels = pick_levels(stop_i - 1 - start_i, knobs.stack_mode == 1);
+    const size_t tables = 4 * kSymCells;
+    auto *counts = reinterpret_cast<unsigned long long *>(d_counts);
+    auto *nodes = reinterpret_cast<unsigned long long *>(d_nodes);
+    int bpsm = 0;
+#define MF_SYM_BATCHED(TPB, LV)                                                                  \
+    do {                                                                                         \
+        const size_t smem = tables + Carve<TPB, 16, LV>::kThreadBytes;                           \
+        e = prepare(sym_batched_kernel<TPB, LV>, smem, TPB, knobs.blocks_per_sm, bpsm);          \
+        if (e != cudaSuccess) return e;                                                          \
+        const unsigned long long threads = 1ULL * sms * bpsm * TPB;                             \
+        const unsigned long long hungry = threads * knobs.hungry_factor / 8;                    \
+        sym_batched_kernel<TPB, LV><<<unsigned(sms * bpsm), TPB, smem, stream>>>(                \
+            d_edges, src, num, counts, nodes, Q, knobs.node_budget, hungry, knobs.wait_limit);  \
+    } while (0)
+    if (knobs.block_threads == 256) {
+        switch (levels) {
+            case 24: MF_SYM_BATCHED(256, 24); break;
+            case 32: MF_SYM_BATCHED(256, 32); break;
+            case 48: MF_SYM_BATCHED(256, 48); break;
+            default: MF_SYM_BATCHED(256, 0); break;
+        }
+    } else {
+        switch (levels) {
+            case 24: MF_SYM_BATCHED(128, 24); break;
+            case 32: MF_SYM_BATCHED(128, 32); break;
+            case 48: MF_SYM_BATCHED(128, 48); break;
+            default: MF_SYM_BATCHED(128, 0); break;
+        }
     }
 #undef MF_SYM_BATCHED
     return cudaGetLastError();
 }
 
 cudaError_t launch_lunnon_batched(const uint8_t *d_tables, uint32_t tables_bytes,
-                                  const LunnonInstanceDev *d_inst, int num_inst,
+                                  const LunnonInstanceDev *d_inst, int num_inst, int max_levels,
                                   const uint8_t *d_states, const uint32_t *d_state_owner,
                                   uint64_t num, uint64_t *d_counts, uint64_t *d_nodes,
                                   void *d_workspace, const BatchKnobs &knobs, cudaStream_t stream) {
     Queue Q = carve_queue(d_workspace, knobs.queue_capacity);
-    cudaError_t e = cudaMemsetAsync(d_workspace, 0, 256, stream);
-    if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(Q.ready, 0, knobs.queue_capacity * sizeof(unsigned int), stream);
+    cudaError_t e = reset_queue(Q, stream);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(d_counts, 0, size_t(num_inst) * sizeof(uint64_t), stream);
     if (e != cudaSuccess) return e;
     if (num == 0) return cudaSuccess;
     const int sms = device_sm_count();
     const uint32_t tb = (tables_bytes + 15) / 16 * 16;
-    const unsigned long long threads = 1ULL * sms * knobs.blocks_per_sm * knobs.block_threads;
-    const unsigned long long hungry = threads * knobs.hungry_factor / 8;
-    const unsigned grid = unsigned(sms * knobs.blocks_per_sm);
-    const size_t smem = size_t(17) * 4 * knobs.block_threads + tb;
-#define MF_LUN_BATCHED(TPB)                                                                     \
-    do {                                                                                        \
-        cudaFuncSetAttribute(lunnon_batched_kernel<TPB>,                                        \
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);          \
-        lunnon_batched_kernel<TPB><<<grid, TPB, smem, stream>>>(                                \
-            LunnonSource{d_states, d_state_owner, d_inst, d_tables, lunnon_state_stride(64)},   \
-            tb, num, reinterpret_cast<unsigned long long *>(d_counts),                          \
-            reinterpret_cast<unsigned long long *>(d_nodes), Q, knobs.node_budget, hungry,      \
-            knobs.wait_limit);                                                                  \
+    const LunnonSource src{d_states, d_state_owner, d_inst, lunnon_state_stride(64)};
+    const int levels = pick_levels(max_levels, knobs.stack_mode == 1);
+    auto *counts = reinterpret_cast<unsigned long long *>(d_counts);
+    auto *nodes = reinterpret_cast<unsigned long long *>(d_nodes);
+    int bpsm = 0;
+#define MF_LUN_BATCHED(TPB, LV)                                                                  \
+    do {                                                                                         \
+        const size_t smem = tb + Carve<TPB, 17, LV>::kThreadBytes;                               \
+        e = prepare(lunnon_batched_kernel<TPB, LV>, smem, TPB, knobs.blocks_per_sm, bpsm);       \
+        if (e != cudaSuccess) return e;                                                          \
+        const unsigned long long threads = 1ULL * sms * bpsm * TPB;                             \
+        const unsigned long long hungry = threads * knobs.hungry_factor / 8;                    \
+        lunnon_batched_kernel<TPB, LV><<<unsigned(sms * bpsm), TPB, smem, stream>>>(             \
+            d_tables, tb, src, num, counts, nodes, Q, knobs.node_budget, hungry,                \
+            knobs.wait_limit);                                                                   \
     } while (0)
-    switch (knobs.block_threads) {
-        case 64: MF_LUN_BATCHED(64); break;
-        case 256: MF_LUN_BATCHED(256); break;
-        default: MF_LUN_BATCHED(128); break;
+    if (knobs.block_threads == 256) {
+        switch (levels) {
+            case 24: MF_LUN_BATCHED(256, 24); break;
+            case 32: MF_LUN_BATCHED(256, 32); break;
+            case 48: MF_LUN_BATCHED(256, 48); break;
+            default: MF_LUN_BATCHED(256, 0); break;
+        }
+    } else {
+        switch (levels) {
+            case 24: MF_LUN_BATCHED(128, 24); break;
+            case 32: MF_LUN_BATCHED(128, 32); break;
+            case 48: MF_LUN_BATCHED(128, 48); break;
+            default: MF_LUN_BATCHED(128, 0); break;
+        }
     }
 #undef MF_LUN_BATCHED
     return cudaGetLastError();

@@ -104,6 +104,7 @@ struct BatchKnobs {
     uint32_t hungry_factor;
     uint64_t queue_capacity;
     uint32_t wait_limit;
+    uint32_t stack_mode;  // 0: shared memory when it fits, 1: local memory
 };
 BatchKnobs resolve_knobs(const mf_batch_config *cfg);
 
@@ -139,10 +140,11 @@ struct LunnonInstanceDev {
     int32_t start_leaf;
 };
 
-cudaError_t launch_sym_plain(const uint8_t *edges, int start_i, int stop_i, const uint8_t *d_cycles,
-                             uint64_t num, uint64_t *d_counts, uint64_t *d_nodes,
-                             cudaStream_t stream);
-cudaError_t launch_sym_batched(const uint8_t *edges, int start_i, int stop_i,
+// d_edges: the 4 x 64 edge pages in device memory.
+cudaError_t launch_sym_plain(const uint8_t *d_edges, int start_i, int stop_i,
+                             const uint8_t *d_cycles, uint64_t num, uint64_t *d_counts,
+                             uint64_t *d_nodes, cudaStream_t stream);
+cudaError_t launch_sym_batched(const uint8_t *d_edges, int start_i, int stop_i,
                                const uint8_t *d_cycles, uint64_t num, uint64_t *d_counts,
                                uint64_t *d_nodes, void *d_workspace, const BatchKnobs &knobs,
                                cudaStream_t stream);
@@ -152,8 +154,9 @@ cudaError_t launch_lunnon_plain(const uint8_t *d_table, int n, int dim, int star
                                 cudaStream_t stream);
 // Batched multi-instance Lunnon: states of all instances concatenated;
 // d_state_owner[k] = instance of state k; d_counts[instance] += count/leaf.
+// max_levels: the largest n - start_leaf over the instances.
 cudaError_t launch_lunnon_batched(const uint8_t *d_tables, uint32_t tables_bytes,
-                                  const LunnonInstanceDev *d_inst, int num_inst,
+                                  const LunnonInstanceDev *d_inst, int num_inst, int max_levels,
                                   const uint8_t *d_states, const uint32_t *d_state_owner,
                                   uint64_t num, uint64_t *d_counts, uint64_t *d_nodes,
                                   void *d_workspace, const BatchKnobs &knobs, cudaStream_t stream);
