@@ -295,6 +295,39 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_profile_case(case: str):
+    """One launch of each kernel on a small case, for ncu (a few seconds of
+    GPU work, inputs ~28 MB): `sym-partial` counts the 433,131 7x7 cases from
+    24 to 30 cells (plain kernel, then batched); `lunnon` counts the 6x6 map
+    from its 18-leaf prefix states (plain, then batched)."""
+    import numpy as np
+    import torch
+
+    import map_folding_gb300 as mf
+    from map_folding_gb300 import build as mfbuild
+
+    if not mfbuild.LIB.exists():
+        mfbuild.build()
+    if case == "sym-partial":
+        plan = mf.SymPlan(N, EXPANDED_N)
+        cycles, _ = plan.cases()
+        d_cyc = torch.from_numpy(np.ascontiguousarray(cycles)).cuda()
+        d_counts = torch.zeros(len(cycles), dtype=torch.int64, device="cuda")
+        ws = torch.empty(mf.sym_workspace_bytes(), dtype=torch.uint8, device="cuda")
+        mf.count_cases_device(N, EXPANDED_N, 30, d_cyc.data_ptr(), len(cycles), d_counts.data_ptr())
+        mf.count_cases_batched_device(N, EXPANDED_N, 30, d_cyc.data_ptr(), len(cycles),
+                                      d_counts.data_ptr(), ws.data_ptr(), ws.numel())
+    elif case == "lunnon":
+        plan = mf.LunnonPlan((6, 6))
+        for mode in ("plain", "batched"):
+            count, _, _ = plan.count(18, mode)
+            assert count == 123912532224
+    else:
+        raise SystemExit(f"unknown profile case {case}")
+    torch.cuda.synchronize()
+    print(f"profile case {case} done")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -304,8 +337,11 @@ def main():
     ap.add_argument("--plain", action="store_true", default=True)
     ap.add_argument("--no-plain", dest="plain", action="store_false")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-case", default="", help="run one small case for ncu and exit")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_case:
+        run_profile_case(args.profile_case)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

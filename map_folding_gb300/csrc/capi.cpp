@@ -391,7 +391,8 @@ static int32_t lunnon_batch_impl(const mf_lunnon_plan *const *plans, int32_t num
     cudaEventRecord(tk.a, st);
     int max_levels = 0;
     for (const auto &I : inst) max_levels = std::max(max_levels, I.n - I.start_leaf);
-    MF_TRY_CUDA(launch_lunnon_batched(d_meta, uint32_t(tables.size()), d_inst, num_plans,
+    const uint32_t meta_used = uint32_t(tables.size() + inst.size() * sizeof(LunnonInstanceDev));
+    MF_TRY_CUDA(launch_lunnon_batched(d_meta, meta_used, uint32_t(tables.size()), num_plans,
                                       max_levels, d_units,
                                       reinterpret_cast<uint32_t *>(d_units + unit_bytes), total,
                                       d_counts, d_counts + num_plans, d_work, knobs, st));

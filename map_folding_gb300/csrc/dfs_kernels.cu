@@ -90,14 +90,16 @@ __device__ __forceinline__ bool list_valid(const List<TPB> &L, int placed) {
 // for its longest lane's total walk, not for the sum of per-page maxima.
 struct SymRules {
     const uint8_t *edge;  // 4 pages x 64, shared memory
+    const uint32_t *nb4;  // per cell: its 4 page neighbours, one byte each
     template <int TPB>
     __device__ __forceinline__ uint64_t gaps(const List<TPB> &L, int i,
                                              unsigned long long &nodes) const {
         ++nodes;
         uint64_t good = low_bits(i);
-        unsigned pend = 0;  // pages whose neighbour of i is placed
-#pragma unroll
-        for (int p = 0; p < 4; ++p) pend |= unsigned(edge[p * kSymCells + i] < i) << p;
+        // Pages whose neighbour of i is placed: one word, four byte compares.
+        const uint32_t nb = nb4[i];
+        const uint32_t placed = __vcmpltu4(nb, 0x01010101u * uint32_t(i)) & 0x01010101u;
+        unsigned pend = (placed * 0x01020408u) >> 24;
         const uint8_t *e = edge;
         uint64_t allowed = ~0ULL;
         int other = 0, j = 0;
@@ -108,7 +110,7 @@ struct SymRules {
                 const int p = __ffs(pend) - 1;
                 pend &= pend - 1;
                 e = edge + p * kSymCells;
-                other = e[i];
+                other = (nb >> (8 * p)) & 0xff;
                 allowed = 1ULL << other;
                 j = L.get(other);
                 continue;
@@ -343,6 +345,25 @@ __device__ __forceinline__ void run_units(const Rules &R, const List<TPB> &L, St
 
 // ------------------------------------------------------- plain kernels ---
 
+// Sym tables in shared memory: the 4 edge pages (256 B), then each cell's 4
+// page neighbours packed into one word (256 B).
+constexpr size_t kSymTables = 8 * kSymCells;
+
+template <int TPB>
+__device__ __forceinline__ void stage_sym_tables(uint8_t *smem, const uint8_t *__restrict__ edges) {
+    for (int k = threadIdx.x; k < 64; k += TPB) {
+        reinterpret_cast<uint32_t *>(smem)[k] = __ldg(reinterpret_cast<const uint32_t *>(edges) + k);
+        reinterpret_cast<uint32_t *>(smem + 4 * kSymCells)[k] =
+            uint32_t(__ldg(edges + k)) | (uint32_t(__ldg(edges + kSymCells + k)) << 8) |
+            (uint32_t(__ldg(edges + 2 * kSymCells + k)) << 16) |
+            (uint32_t(__ldg(edges + 3 * kSymCells + k)) << 24);
+    }
+}
+
+__device__ __forceinline__ SymRules sym_rules(const uint8_t *smem) {
+    return SymRules{smem, reinterpret_cast<const uint32_t *>(smem + 4 * kSymCells)};
+}
+
 // One thread per case: d_counts[k] = completions of case k (UINT64_MAX if
 // its cycle is malformed).  Shared memory: 4 edge pages, then the carve.
 template <int TPB, int LEVELS>
@@ -352,13 +373,11 @@ __global__ void __launch_bounds__(TPB)
                      unsigned long long *__restrict__ counts,
                      unsigned long long *__restrict__ nodes_out) {
     extern __shared__ __align__(16) uint8_t smem[];
-    constexpr size_t kTables = 4 * kSymCells;
     using C = Carve<TPB, 16, LEVELS>;
-    for (int k = threadIdx.x; k < 64; k += TPB)
-        reinterpret_cast<uint32_t *>(smem)[k] = __ldg(reinterpret_cast<const uint32_t *>(edges) + k);
-    const List<TPB> L = C::list(smem, kTables);
+    stage_sym_tables<TPB>(smem, edges);
+    const List<TPB> L = C::list(smem, kSymTables);
     typename StackOf<TPB, LEVELS>::type S;
-    init_stack<TPB, 16, LEVELS>(S, smem, kTables);
+    init_stack<TPB, 16, LEVELS>(S, smem, kSymTables);
     const uint64_t unit = uint64_t(blockIdx.x) * TPB + threadIdx.x;
     const bool active = unit < num;
     if (active) load_list<TPB, 16>(L, cycles + unit * kSymCells, kSymCells);
@@ -367,7 +386,7 @@ __global__ void __launch_bounds__(TPB)
     unsigned long long nodes = 0, leaves = 0;
     const bool bad = active && !list_valid(L, start_i);
     S.base = start_i;
-    run_units(SymRules{smem}, L, S, active && !bad, start_i, stop_i - 1, leaves, nodes);
+    run_units(sym_rules(smem), L, S, active && !bad, start_i, stop_i - 1, leaves, nodes);
     if (active) counts[unit] = bad ? ~0ULL : leaves;
     if (nodes_out) {
         const unsigned long long s = warp_sum(nodes);
@@ -431,62 +450,55 @@ __device__ __forceinline__ unsigned long long vload(const unsigned long long *p)
     return *reinterpret_cast<const volatile unsigned long long *>(p);
 }
 
-__device__ __forceinline__ bool ring_push(const Queue &Q, const uint32_t (&w)[24]) {
-    unsigned long long pos = vload(&Q.hdr->spawn_tail);
-    for (int attempt = 0; attempt < 64; ++attempt) {
-        const unsigned long long cell = pos & (Q.capacity - 1);
-        const long long diff = (long long)(vload(Q.seq + cell) - pos);
-        if (diff == 0) {
-            const unsigned long long seen = atomicCAS(&Q.hdr->spawn_tail, pos, pos + 1);
-            if (seen == pos) {
-                uint4 *dst = reinterpret_cast<uint4 *>(Q.slots + cell);
-#pragma unroll
-                for (int q = 0; q < 6; ++q)
-                    __stcg(dst + q, make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]));
-                __threadfence();
-                atomicExch(Q.seq + cell, pos + 1);
-                return true;
-            }
-            pos = seen;
-        } else if (diff < 0) {
-            return false;  // full
-        } else {
-            pos = vload(&Q.hdr->spawn_tail);
-        }
-    }
-    return false;
+// Warp-cooperative claim of up to `want` (<= 32) consecutive tickets at the
+// ring's head (pop) or tail (push): each lane checks one cell's sequence, and
+// one CAS by lane 0 takes the run of ready cells for the whole warp, so a
+// warp makes at most one atomic per refill or donation round.  All 32 lanes
+// call it; returns the number of tickets taken (warp-uniform), the first in
+// `first`.
+__device__ __forceinline__ int ring_claim(const Queue &Q, unsigned long long *counter, int want,
+                                          bool pop, unsigned long long &first) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long pos = 0;
+    if (lane == 0) pos = vload(counter);
+    pos = __shfl_sync(kFull, pos, 0);
+    const unsigned long long t = pos + lane;
+    const bool ready =
+        lane < want && vload(Q.seq + (t & (Q.capacity - 1))) == (pop ? t + 1 : t);
+    const unsigned ok = __ballot_sync(kFull, ready);
+    const int run = ok == kFull ? 32 : __ffs(~ok) - 1;  // ready cells from lane 0 on
+    int got = 0;
+    if (lane == 0 && run > 0) got = atomicCAS(counter, pos, pos + run) == pos ? run : 0;
+    first = pos;
+    return __shfl_sync(kFull, got, 0);
 }
 
-__device__ __forceinline__ bool ring_pop(const Queue &Q, uint32_t (&w)[24]) {
-    unsigned long long pos = vload(&Q.hdr->spawn_head);
-    for (int attempt = 0; attempt < 64; ++attempt) {
-        const unsigned long long cell = pos & (Q.capacity - 1);
-        const long long diff = (long long)(vload(Q.seq + cell) - (pos + 1));
-        if (diff == 0) {
-            const unsigned long long seen = atomicCAS(&Q.hdr->spawn_head, pos, pos + 1);
-            if (seen == pos) {
-                __threadfence();
-                const uint4 *src = reinterpret_cast<const uint4 *>(Q.slots + cell);
+// Copy ticket t's item out and free its cell for the producer of t + capacity.
+__device__ __forceinline__ void ring_take(const Queue &Q, unsigned long long t, uint32_t (&w)[24]) {
+    const unsigned long long cell = t & (Q.capacity - 1);
+    __threadfence();
+    const uint4 *src = reinterpret_cast<const uint4 *>(Q.slots + cell);
 #pragma unroll
-                for (int q = 0; q < 6; ++q) {
-                    const uint4 x = __ldcg(src + q);
-                    w[4 * q] = x.x;
-                    w[4 * q + 1] = x.y;
-                    w[4 * q + 2] = x.z;
-                    w[4 * q + 3] = x.w;
-                }
-                __threadfence();
-                atomicExch(Q.seq + cell, pos + Q.capacity);
-                return true;
-            }
-            pos = seen;
-        } else if (diff < 0) {
-            return false;  // empty
-        } else {
-            pos = vload(&Q.hdr->spawn_head);
-        }
+    for (int q = 0; q < 6; ++q) {
+        const uint4 x = __ldcg(src + q);
+        w[4 * q] = x.x;
+        w[4 * q + 1] = x.y;
+        w[4 * q + 2] = x.z;
+        w[4 * q + 3] = x.w;
     }
-    return false;
+    __threadfence();
+    atomicExch(Q.seq + cell, t + Q.capacity);
+}
+
+// Write ticket t's item and publish it to its consumer.
+__device__ __forceinline__ void ring_put(const Queue &Q, unsigned long long t, const uint32_t (&w)[24]) {
+    const unsigned long long cell = t & (Q.capacity - 1);
+    uint4 *dst = reinterpret_cast<uint4 *>(Q.slots + cell);
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+        __stcg(dst + q, make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]));
+    __threadfence();
+    atomicExch(Q.seq + cell, t + 1);
 }
 
 __global__ void ring_init_kernel(unsigned long long *seq, unsigned long long capacity) {
@@ -508,22 +520,29 @@ struct LunnonSource {
     uint32_t stride;
 };
 
-// The persistent loop, in lockstep rounds.  Each round: idle lanes refill
-// (initial units through one warp-aggregated atomicAdd, then split items),
-// every busy lane evaluates one node, consumes it and advances to its next
-// node.  Every `period` rounds the warp accounts finished units and, once
-// the initial units are handed out and the queue is running dry, lets each
-// busy lane give away its shallowest untried siblings.  A warp leaves when it
-// is idle and all work is accounted for, or when it has stayed idle for
-// wait_limit rounds -- leaving is always safe, because the warp that owns a
-// split item's parent keeps looping until it has nothing left.
+// The persistent loop, in lockstep rounds.  Each round every busy lane
+// evaluates one node, consumes it and advances to its next node; a lane whose
+// unit is exhausted starts its next one at once from a one-unit-ahead
+// prefetch (the index is taken with an atomicAdd when the previous unit
+// starts, the record is loaded into registers at the next bookkeeping round,
+// so neither latency is paid when the unit is needed).  Every `period` rounds
+// a warp does its bookkeeping: it reports finished units and its idle-lane
+// count, lets idle lanes take split items, and -- while fewer split items are
+// queued than lanes wait for work -- lets a few busy lanes give away their
+// shallowest untried siblings.  A warp leaves when it is idle and all work is
+// accounted for, or when it has stayed idle for wait_limit rounds; leaving is
+// always safe, because the warp that owns a split item's parent keeps looping
+// until it has nothing left.
 template <int TPB, int WORDS, bool kSym, class Stk>
-__device__ __forceinline__ void persistent_loop(const uint8_t *s_tables, const SymSource &sym,
-                                                const LunnonSource &lun, unsigned long long num,
+__device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
+                                                const LunnonInstanceDev *s_inst,
+                                                const SymSource &sym, const LunnonSource &lun,
+                                                unsigned long long num,
                                                 unsigned long long *counts,
                                                 unsigned long long *nodes_out, const Queue &Q,
-                                                uint32_t period, unsigned long long hungry_level,
-                                                uint32_t wait_limit, const List<TPB> &L, Stk &S) {
+                                                uint32_t period, uint32_t wait_limit,
+                                                const List<TPB> &L, Stk &S) {
+    constexpr int kVecs = (WORDS + 3) / 4;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
     bool busy = false, fresh = false;
@@ -531,11 +550,34 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables, const S
     uint32_t owner = 0;
     unsigned long long leaves = 0, nodes = 0, finished = 0, started = 0;
     uint32_t idle_rounds = 0, round = 0;
-    bool tail_phase = false;  // all initial units handed out
-    const SymRules srules{s_tables};
+    int reported_idle = 0;  // lane 0: idle lanes this warp last reported
+    bool ring_hint = false;  // warp-uniform: the split ring probably has items
+    const SymRules srules = sym_rules(s_tables);
     LunnonRules lrules{s_tables, 0, 0};
 
-    // Count a finished unit into its owner's slot.
+    // Prefetch state: 0 = no initial unit left for this lane, 1 = index
+    // requested, 2 = record requested too.  The first indices come from one
+    // warp-aggregated atomicAdd.
+    unsigned long long pre_k = 0;
+    {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(&Q.hdr->init_next, 32ULL);
+        pre_k = __shfl_sync(kFull, base, 0) + lane;
+    }
+    int pre_stage = 1;
+    uint4 pre[kVecs];
+    uint32_t pre_owner = 0;
+
+#define MF_FETCH_RECORD()                                                                   \
+    do {                                                                                   \
+        const uint4 *src_ = kSym                                                           \
+            ? reinterpret_cast<const uint4 *>(sym.cycles + pre_k * kSymCells)              \
+            : reinterpret_cast<const uint4 *>(lun.states + pre_k * lun.stride);            \
+        _Pragma("unroll") for (int q_ = 0; q_ < kVecs; ++q_) pre[q_] = __ldg(src_ + q_);   \
+        if (!kSym) pre_owner = __ldg(lun.state_owner + pre_k);                             \
+        pre_stage = 2;                                                                     \
+    } while (0)
+
     auto flush = [&]() {
         if (leaves) {
             const unsigned long long weight = kSym ? 1ULL : static_cast<unsigned long long>(lrules.n);
@@ -545,78 +587,65 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables, const S
         ++finished;
     };
 
-    auto set_instance = [&](uint32_t inst) {
-        const LunnonInstanceDev I = lun.inst[inst];
+    auto set_instance = [&](uint32_t inst) -> int {
+        const LunnonInstanceDev I = s_inst[inst];
         lrules = LunnonRules{s_tables + I.table_offset, I.n, I.dim};
         last = I.n;
         S.base = I.start_leaf;
-        return I;
+        return I.start_leaf;
     };
 
-    // Load initial unit k; returns true if it needs a search.
-    auto load_initial = [&](unsigned long long k) -> bool {
-        ++started;
-        bool bad;
-        if (kSym) {
-            load_list<TPB, WORDS>(L, sym.cycles + k * kSymCells, kSymCells);
-            owner = uint32_t(k);
-            root = sym.start_i;
-            last = sym.last;
-            S.base = root;
-            bad = !list_valid(L, root);
-        } else {
-            load_list<TPB, WORDS>(L, lun.states + k * lun.stride, lun.stride);
-            owner = lun.state_owner[k];
-            const LunnonInstanceDev I = set_instance(owner);
-            root = I.start_leaf;
-            bad = !list_valid(L, root < I.n + 1 ? root : I.n + 1);
-        }
-        if (bad) {
-            atomicExch(&Q.hdr->error, 1u);
-            ++finished;
-            return false;
-        }
-        if (root > last) {  // nothing left to place: one completion
-            leaves = 1;
-            flush();
-            return false;
-        }
-        lvl = root;
-        eval = root;
-        fresh = true;
-        return true;
-    };
-
-    // Load a split item; returns true if one was available.
-    auto load_split = [&]() -> bool {
-        uint32_t w[24];
-        if (!ring_pop(Q, w)) return false;
-        ++started;
+    // Warp-cooperative intake of split items by the lanes in `need` (all 32
+    // lanes call): one claim on the ring's head, then each taking lane copies
+    // its item.  Returns true if fewer items were available than asked for.
+    auto take_splits = [&](unsigned need) -> bool {
+        const int want = __popc(need);
+        unsigned long long first = 0;
+        const int got = ring_claim(Q, &Q.hdr->spawn_head, want, true, first);
+        const bool mine = (need >> lane) & 1u;
+        const int rank = __popc(need & lt_mask);
+        if (mine && rank < got) {
+            uint32_t w[24];
+            ring_take(Q, first + rank, w);
+            ++started;
 #pragma unroll
-        for (int k2 = 0; k2 < WORDS; ++k2) L.set_word(k2, w[k2]);
-        owner = w[17];
-        root = int(w[20]);
-        if (kSym) {
-            last = sym.last;
-            S.base = sym.start_i;
-        } else {
-            set_instance(owner);
+            for (int k2 = 0; k2 < WORDS; ++k2) L.set_word(k2, w[k2]);
+            owner = w[17];
+            root = int(w[20]);
+            if (kSym) {
+                last = sym.last;
+                S.base = sym.start_i;
+            } else {
+                set_instance(owner);
+            }
+            lvl = root;
+            S.set(root, uint64_t(w[18]) | (uint64_t(w[19]) << 32));
+            eval = advance(L, S, lvl, root);  // an item's mask is never empty
+            fresh = false;
+            busy = eval >= 0;
         }
-        lvl = root;
-        S.set(root, uint64_t(w[18]) | (uint64_t(w[19]) << 32));
-        eval = advance(L, S, lvl, root);  // the item's mask is never empty
-        fresh = false;
-        return eval >= 0;
+        return got < want;
     };
 
-    // Give away the shallowest untried sibling set as a split item.  Items
-    // root..lvl are inserted (lvl's evaluation is pending): roll the list back
-    // to that level, copy it out, replay.
+    // Warp-cooperative donation (all 32 lanes call): every busy lane with an
+    // untried sibling set at least kMinSplitHeight above the counted level
+    // gives the shallowest such set away.  One claim on the ring's tail
+    // reserves cells for all donors; each donor rolls its list back to that
+    // level, copies it out, replays, and publishes.
     auto donate = [&]() {
         int s = root;
-        while (s < lvl && S.get(s) == 0) ++s;
-        const uint64_t m = S.get(s);
-        if (m == 0 || last - s < kMinSplitHeight) return;
+        uint64_t m = 0;
+        if (busy && !fresh) {
+            while (s < lvl && S.get(s) == 0) ++s;
+            m = S.get(s);
+        }
+        const bool can = busy && !fresh && m != 0 && last - s >= kMinSplitHeight;
+        const unsigned donors = __ballot_sync(kFull, can);
+        if (!donors) return;
+        unsigned long long first = 0;
+        const int got = ring_claim(Q, &Q.hdr->spawn_tail, __popc(donors), false, first);
+        const int rank = __popc(donors & lt_mask);
+        if (!can || rank >= got) return;
         for (int l = lvl; l >= s; --l) L.put(S.pick(l), L.get(l));
         uint32_t w[24];
 #pragma unroll
@@ -632,34 +661,84 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables, const S
             L.put(l, L.get(j));
             L.put(j, l);
         }
-        if (ring_push(Q, w)) S.set(s, 0);
+        S.set(s, 0);
+        ring_put(Q, first + rank, w);
     };
 
+    uint32_t nap = 256;  // idle back-off, ns
     for (;;) {
-        // Refill idle lanes: initial units first, one atomic per warp.
-        const unsigned need = __ballot_sync(kFull, !busy);
-        if (need) {
-            unsigned long long base = num;
-            const int leader = __ffs(need) - 1;
-            if (!tail_phase && lane == leader) {
-                if (vload(&Q.hdr->init_next) < num)
-                    base = atomicAdd(&Q.hdr->init_next, (unsigned long long)__popc(need));
-            }
-            base = __shfl_sync(kFull, base, leader);
-            if (base >= num) tail_phase = true;
-            if (!busy) {
-                const unsigned long long k = base + __popc(need & lt_mask);
-                if (k < num) busy = load_initial(k);
-                else if (tail_phase) busy = load_split();
+        // Start the prefetched unit on lanes whose search has ended.
+        if (!busy && pre_stage != 0) {
+            if (pre_k < num) {
+                if (pre_stage == 1) MF_FETCH_RECORD();
+#pragma unroll
+                for (int q = 0; q < kVecs; ++q) {
+                    const uint32_t ws[4] = {pre[q].x, pre[q].y, pre[q].z, pre[q].w};
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (4 * q + k < WORDS) L.set_word(4 * q + k, ws[k]);
+                }
+                ++started;
+                bool ok;
+                if (kSym) {
+                    owner = uint32_t(pre_k);
+                    root = sym.start_i;
+                    last = sym.last;
+                    S.base = root;
+                    ok = list_valid(L, root);
+                } else {
+                    owner = pre_owner;
+                    root = set_instance(owner);
+                    ok = list_valid(L, root < lrules.n + 1 ? root : lrules.n + 1);
+                }
+                if (!ok) {
+                    atomicExch(&Q.hdr->error, 1u);
+                    ++finished;
+                } else if (root > last) {  // nothing left to place: one completion
+                    leaves = 1;
+                    flush();
+                } else {
+                    busy = true;
+                    fresh = true;
+                    lvl = root;
+                    eval = root;
+                }
+                pre_k = atomicAdd(&Q.hdr->init_next, 1ULL);
+                pre_stage = 1;
+            } else {
+                pre_stage = 0;
             }
         }
+        // Lanes without initial units take split items while the warp's hint
+        // says the ring has some (refreshed at bookkeeping, cleared by a miss).
+        if (ring_hint) {
+            const unsigned need = __ballot_sync(kFull, !busy && pre_stage == 0);
+            if (need && take_splits(need)) ring_hint = false;
+        }
+        const bool bookkeeping = ++round >= period;
         if (!__any_sync(kFull, busy)) {
-            // Account this warp's finished units first, then decide.
+            // The whole warp is idle: report, look for split items, decide.
             const unsigned long long f = warp_sum(finished);
             finished = 0;
-            int stop = 0;
             if (lane == 0) {
                 if (f) atomicAdd(&Q.hdr->completed, f);
+                if (reported_idle != 32) {
+                    atomicAdd(reinterpret_cast<unsigned long long *>(&Q.hdr->idle_lanes),
+                              (unsigned long long)(long long)(32 - reported_idle));
+                    reported_idle = 32;
+                }
+            }
+            const unsigned need = __ballot_sync(kFull, pre_stage == 0);
+            if (need) take_splits(need);
+            // A lane still holding a prefetched unit keeps the warp alive.
+            const bool holding = __any_sync(kFull, pre_stage != 0 && pre_k < num);
+            if (__any_sync(kFull, busy) || holding) {
+                idle_rounds = 0;
+                nap = 256;
+                continue;
+            }
+            int stop = 0;
+            if (lane == 0) {
                 const unsigned long long total = num + vload(&Q.hdr->spawn_tail);
                 stop = (vload(&Q.hdr->init_next) >= num && vload(&Q.hdr->completed) >= total) ||
                        *reinterpret_cast<volatile unsigned int *>(&Q.hdr->error) != 0u ||
@@ -667,10 +746,12 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables, const S
             }
             stop = __shfl_sync(kFull, stop, 0);
             if (stop) break;
-            __nanosleep(256);
+            __nanosleep(nap);
+            if (nap < 8192) nap <<= 1;
             continue;
         }
         idle_rounds = 0;
+        nap = 256;
         // One evaluation per busy lane.
         if (busy) {
             uint64_t g;
@@ -687,27 +768,42 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables, const S
                 busy = false;
             }
         }
-        // Bookkeeping every `period` rounds.
-        if (++round >= period) {
-            round = 0;
-            const unsigned long long f = warp_sum(finished);
-            finished = 0;
-            int hungry = 0, tail = tail_phase;
-            if (lane == 0) {
-                if (f) atomicAdd(&Q.hdr->completed, f);
-                if (!tail) tail = vload(&Q.hdr->init_next) >= num;
-                if (tail) {
-                    const unsigned long long queued =
-                        vload(&Q.hdr->spawn_tail) - vload(&Q.hdr->spawn_head);
-                    hungry = queued < hungry_level;
-                }
-            }
-            tail_phase = __shfl_sync(kFull, tail, 0) != 0;
-            hungry = __shfl_sync(kFull, hungry, 0);
-            if (hungry && busy && !fresh) donate();
+        if (!bookkeeping) continue;
+        round = 0;
+        // Prefetched indices have long arrived: request their records.
+        if (pre_stage == 1) {
+            if (pre_k < num) MF_FETCH_RECORD();
+            else pre_stage = 0;
         }
+        const unsigned idle_mask = __ballot_sync(kFull, !busy);
+        const unsigned long long f = warp_sum(finished);
+        finished = 0;
+        long long want = 0, queued = 0;
+        if (lane == 0) {
+            if (f) atomicAdd(&Q.hdr->completed, f);
+            const int idle_now = __popc(idle_mask);
+            if (idle_now != reported_idle) {
+                atomicAdd(reinterpret_cast<unsigned long long *>(&Q.hdr->idle_lanes),
+                          (unsigned long long)(long long)(idle_now - reported_idle));
+                reported_idle = idle_now;
+            }
+            if (vload(&Q.hdr->init_next) >= num) {
+                queued = (long long)(vload(&Q.hdr->spawn_tail) - vload(&Q.hdr->spawn_head));
+                const long long waiting = *reinterpret_cast<volatile long long *>(&Q.hdr->idle_lanes);
+                want = waiting - queued;
+            }
+        }
+        want = __shfl_sync(kFull, want, 0);
+        ring_hint = __shfl_sync(kFull, queued, 0) > 0;
+        // Feed waiting lanes: busy lanes give away their shallowest untried
+        // siblings while lanes wait for work.
+        if (want > 0) donate();
     }
+#undef MF_FETCH_RECORD
 
+    if (lane == 0 && reported_idle)
+        atomicAdd(reinterpret_cast<unsigned long long *>(&Q.hdr->idle_lanes),
+                  (unsigned long long)(-(long long)reported_idle));
     const unsigned long long ns = warp_sum(nodes);
     const unsigned long long st = warp_sum(started);
     if (lane == 0) {
@@ -720,38 +816,38 @@ template <int TPB, int LEVELS>
 __global__ void __launch_bounds__(TPB)
     sym_batched_kernel(const uint8_t *__restrict__ edges, SymSource src, unsigned long long num,
                        unsigned long long *counts, unsigned long long *nodes_out, Queue Q,
-                       uint32_t period, unsigned long long hungry_level, uint32_t wait_limit) {
+                       uint32_t period, uint32_t wait_limit) {
     extern __shared__ __align__(16) uint8_t smem[];
-    constexpr size_t kTables = 4 * kSymCells;
     using C = Carve<TPB, 16, LEVELS>;
-    for (int k = threadIdx.x; k < 64; k += TPB)
-        reinterpret_cast<uint32_t *>(smem)[k] = __ldg(reinterpret_cast<const uint32_t *>(edges) + k);
+    stage_sym_tables<TPB>(smem, edges);
     __syncthreads();
-    const List<TPB> L = C::list(smem, kTables);
+    const List<TPB> L = C::list(smem, kSymTables);
     typename StackOf<TPB, LEVELS>::type S;
-    init_stack<TPB, 16, LEVELS>(S, smem, kTables);
+    init_stack<TPB, 16, LEVELS>(S, smem, kSymTables);
     LunnonSource none{};
-    persistent_loop<TPB, 16, true>(smem, src, none, num, counts, nodes_out, Q, period,
-                                   hungry_level, wait_limit, L, S);
+    persistent_loop<TPB, 16, true>(smem, nullptr, src, none, num, counts, nodes_out, Q, period,
+                                   wait_limit, L, S);
 }
 
+// Shared memory: the maps' neighbour tables and their instance records
+// (meta_bytes in all, records at inst_offset), then the carve.
 template <int TPB, int LEVELS>
 __global__ void __launch_bounds__(TPB)
-    lunnon_batched_kernel(const uint8_t *__restrict__ tables, uint32_t tables_bytes,
-                          LunnonSource src, unsigned long long num, unsigned long long *counts,
-                          unsigned long long *nodes_out, Queue Q, uint32_t period,
-                          unsigned long long hungry_level, uint32_t wait_limit) {
+    lunnon_batched_kernel(const uint8_t *__restrict__ meta, uint32_t meta_bytes,
+                          uint32_t inst_offset, LunnonSource src, unsigned long long num,
+                          unsigned long long *counts, unsigned long long *nodes_out, Queue Q,
+                          uint32_t period, uint32_t wait_limit) {
     extern __shared__ __align__(16) uint8_t smem[];
     using C = Carve<TPB, 17, LEVELS>;
-    for (uint32_t k = threadIdx.x; k < tables_bytes / 4; k += TPB)
-        reinterpret_cast<uint32_t *>(smem)[k] = __ldg(reinterpret_cast<const uint32_t *>(tables) + k);
+    for (uint32_t k = threadIdx.x; k < meta_bytes / 4; k += TPB)
+        reinterpret_cast<uint32_t *>(smem)[k] = __ldg(reinterpret_cast<const uint32_t *>(meta) + k);
     __syncthreads();
-    const List<TPB> L = C::list(smem, tables_bytes);
+    const List<TPB> L = C::list(smem, meta_bytes);
     typename StackOf<TPB, LEVELS>::type S;
-    init_stack<TPB, 17, LEVELS>(S, smem, tables_bytes);
+    init_stack<TPB, 17, LEVELS>(S, smem, meta_bytes);
     SymSource none{};
-    persistent_loop<TPB, 17, false>(smem, none, src, num, counts, nodes_out, Q, period,
-                                    hungry_level, wait_limit, L, S);
+    persistent_loop<TPB, 17, false>(smem, reinterpret_cast<const LunnonInstanceDev *>(smem + inst_offset),
+                                    none, src, num, counts, nodes_out, Q, period, wait_limit, L, S);
 }
 
 // ------------------------------------------------------- launch helpers --
@@ -830,7 +926,7 @@ cudaError_t launch_sym_plain(const uint8_t *d_edges, int start_i, int stop_i,
     constexpr int TPB = 128;
     const uint64_t blocks = (num + TPB - 1) / TPB;
     const int levels = pick_levels(stop_i - 1 - start_i);
-    const size_t tables = 4 * kSymCells;
+    const size_t tables = kSymTables;
     auto *counts = reinterpret_cast<unsigned long long *>(d_counts);
     auto *nodes = reinterpret_cast<unsigned long long *>(d_nodes);
     int bpsm = 0;
@@ -896,7 +992,7 @@ cudaError_t launch_sym_batched(const uint8_t *d_edges, int start_i, int stop_i,
     const int sms = device_sm_count();
     const SymSource src{d_cycles, start_i, stop_i - 1};
     const int levels = pick_levels(stop_i - 1 - start_i, knobs.stack_mode == 1);
-    const size_t tables = 4 * kSymCells;
+    const size_t tables = kSymTables;
     auto *counts = reinterpret_cast<unsigned long long *>(d_counts);
     auto *nodes = reinterpret_cast<unsigned long long *>(d_nodes);
     int bpsm = 0;
@@ -905,10 +1001,8 @@ cudaError_t launch_sym_batched(const uint8_t *d_edges, int start_i, int stop_i,
         const size_t smem = tables + Carve<TPB, 16, LV>::kThreadBytes;                           \
         e = prepare(sym_batched_kernel<TPB, LV>, smem, TPB, knobs.blocks_per_sm, bpsm);          \
         if (e != cudaSuccess) return e;                                                          \
-        const unsigned long long threads = 1ULL * sms * bpsm * TPB;                             \
-        const unsigned long long hungry = threads * knobs.hungry_factor / 8;                    \
         sym_batched_kernel<TPB, LV><<<unsigned(sms * bpsm), TPB, smem, stream>>>(                \
-            d_edges, src, num, counts, nodes, Q, knobs.node_budget, hungry, knobs.wait_limit);  \
+            d_edges, src, num, counts, nodes, Q, knobs.node_budget, knobs.wait_limit);          \
     } while (0)
     if (knobs.block_threads == 256) {
         switch (levels) {
@@ -929,11 +1023,11 @@ cudaError_t launch_sym_batched(const uint8_t *d_edges, int start_i, int stop_i,
     return cudaGetLastError();
 }
 
-cudaError_t launch_lunnon_batched(const uint8_t *d_tables, uint32_t tables_bytes,
-                                  const LunnonInstanceDev *d_inst, int num_inst, int max_levels,
-                                  const uint8_t *d_states, const uint32_t *d_state_owner,
-                                  uint64_t num, uint64_t *d_counts, uint64_t *d_nodes,
-                                  void *d_workspace, const BatchKnobs &knobs, cudaStream_t stream) {
+cudaError_t launch_lunnon_batched(const uint8_t *d_meta, uint32_t meta_bytes, uint32_t inst_offset,
+                                  int num_inst, int max_levels, const uint8_t *d_states,
+                                  const uint32_t *d_state_owner, uint64_t num, uint64_t *d_counts,
+                                  uint64_t *d_nodes, void *d_workspace, const BatchKnobs &knobs,
+                                  cudaStream_t stream) {
     Queue Q = carve_queue(d_workspace, knobs.queue_capacity);
     cudaError_t e = reset_queue(Q, stream);
     if (e != cudaSuccess) return e;
@@ -941,21 +1035,19 @@ cudaError_t launch_lunnon_batched(const uint8_t *d_tables, uint32_t tables_bytes
     if (e != cudaSuccess) return e;
     if (num == 0) return cudaSuccess;
     const int sms = device_sm_count();
-    const uint32_t tb = (tables_bytes + 15) / 16 * 16;
-    const LunnonSource src{d_states, d_state_owner, d_inst, lunnon_state_stride(64)};
+    const uint32_t mb = (meta_bytes + 15) / 16 * 16;
+    const LunnonSource src{d_states, d_state_owner, nullptr, lunnon_state_stride(64)};
     const int levels = pick_levels(max_levels, knobs.stack_mode == 1);
     auto *counts = reinterpret_cast<unsigned long long *>(d_counts);
     auto *nodes = reinterpret_cast<unsigned long long *>(d_nodes);
     int bpsm = 0;
 #define MF_LUN_BATCHED(TPB, LV)                                                                  \
     do {                                                                                         \
-        const size_t smem = tb + Carve<TPB, 17, LV>::kThreadBytes;                               \
+        const size_t smem = mb + Carve<TPB, 17, LV>::kThreadBytes;                               \
         e = prepare(lunnon_batched_kernel<TPB, LV>, smem, TPB, knobs.blocks_per_sm, bpsm);       \
         if (e != cudaSuccess) return e;                                                          \
-        const unsigned long long threads = 1ULL * sms * bpsm * TPB;                             \
-        const unsigned long long hungry = threads * knobs.hungry_factor / 8;                    \
         lunnon_batched_kernel<TPB, LV><<<unsigned(sms * bpsm), TPB, smem, stream>>>(             \
-            d_tables, tb, src, num, counts, nodes, Q, knobs.node_budget, hungry,                \
+            d_meta, mb, inst_offset, src, num, counts, nodes, Q, knobs.node_budget,             \
             knobs.wait_limit);                                                                   \
     } while (0)
     if (knobs.block_threads == 256) {

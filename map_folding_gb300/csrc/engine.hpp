@@ -125,8 +125,10 @@ struct QueueHeader {
     unsigned long long spawn_tail;  // split items reserved
     unsigned long long completed;   // work items finished
     unsigned long long tasks_run;
-    unsigned int error;             // 1: a bounded wait ran out
-    unsigned int pad[5];
+    unsigned int error;             // 1: a malformed unit was seen
+    unsigned int pad;
+    long long idle_lanes;           // lanes waiting for work (warps report deltas)
+    long long reserved;
 };
 static_assert(sizeof(QueueHeader) == 64, "queue header layout");
 
@@ -154,12 +156,14 @@ cudaError_t launch_lunnon_plain(const uint8_t *d_table, int n, int dim, int star
                                 cudaStream_t stream);
 // Batched multi-instance Lunnon: states of all instances concatenated;
 // d_state_owner[k] = instance of state k; d_counts[instance] += count/leaf.
-// max_levels: the largest n - start_leaf over the instances.
-cudaError_t launch_lunnon_batched(const uint8_t *d_tables, uint32_t tables_bytes,
-                                  const LunnonInstanceDev *d_inst, int num_inst, int max_levels,
-                                  const uint8_t *d_states, const uint32_t *d_state_owner,
-                                  uint64_t num, uint64_t *d_counts, uint64_t *d_nodes,
-                                  void *d_workspace, const BatchKnobs &knobs, cudaStream_t stream);
+// d_meta holds the maps' neighbour tables followed, at inst_offset, by their
+// LunnonInstanceDev records (meta_bytes in all); max_levels is the largest
+// n - start_leaf over the instances.
+cudaError_t launch_lunnon_batched(const uint8_t *d_meta, uint32_t meta_bytes, uint32_t inst_offset,
+                                  int num_inst, int max_levels, const uint8_t *d_states,
+                                  const uint32_t *d_state_owner, uint64_t num, uint64_t *d_counts,
+                                  uint64_t *d_nodes, void *d_workspace, const BatchKnobs &knobs,
+                                  cudaStream_t stream);
 
 int device_sm_count();
 
