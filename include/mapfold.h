@@ -199,6 +199,35 @@ int32_t mf_sym_plan_solve(const mf_sym_plan *plan, uint64_t max_cases, uint64_t 
                           int32_t mode, const mf_batch_config *cfg, uint64_t *answer_lo_hi,
                           mf_run_stats *stats);
 
+/* ---- CUDA-graph replay ------------------------------------------------ */
+
+typedef struct mf_graph mf_graph;
+
+/* Records one batched sym count on fixed device buffers -- node-counter
+ * reset, split-ring reset, per-case count reset, persistent kernel -- into
+ * a CUDA graph, so repeated counts (benchmark steps, chunk rounds) replay
+ * with a single mf_graph_launch.  Arguments as mf_sym_count_cases_batched;
+ * the buffers must stay valid for the graph's lifetime.
+ * No reference counterpart (the reference relaunches per batch,
+ * gpu_folding_v2.cu:512-533). */
+int32_t mf_sym_graph_create(int32_t n, int32_t start_i, int32_t stop_i, const uint8_t *d_cycles,
+                            uint64_t num_cases, uint64_t *d_counts, uint64_t *d_nodes,
+                            void *d_workspace, uint64_t workspace_bytes,
+                            const mf_batch_config *cfg, mf_graph **out);
+int32_t mf_graph_launch(mf_graph *graph, void *stream);
+void mf_graph_destroy(mf_graph *graph);
+
+/* A prepared uneven batch: the maps' prefix states, tables and work queue
+ * resident on the device and the batched launch recorded as a CUDA graph;
+ * mf_lunnon_batch_run replays it and copies the per-map counts back.
+ * Same semantics as mf_lunnon_batch_count. */
+typedef struct mf_lunnon_batch mf_lunnon_batch;
+int32_t mf_lunnon_batch_create(const mf_lunnon_plan *const *plans, int32_t num_plans,
+                               const int32_t *depths, const mf_batch_config *cfg,
+                               mf_lunnon_batch **out);
+int32_t mf_lunnon_batch_run(mf_lunnon_batch *batch, uint64_t *counts_out, mf_run_stats *stats);
+void mf_lunnon_batch_destroy(mf_lunnon_batch *batch);
+
 /* The whole `sym_fold n threads max_cases start_case` computation with the
  * MF_EXPANDED_N semantics: answer = n*n * sum(multiplier * count) over the
  * selected cases (n <= 5: 2*n*n*count).  mode 0 = plain kernel, 1 =

@@ -7,8 +7,10 @@ is the Python mirror of that ABI plus the chunk-sweep driver.
 from .api import (  # noqa: F401
     BatchConfig,
     EngineError,
+    LunnonBatch,
     LunnonPlan,
     RunStats,
+    SymGraph,
     SymPlan,
     count_cases_batched_device,
     count_cases_device,

@@ -156,6 +156,75 @@ def lunnon_batch_count(shapes: Iterable[Sequence[int]], depths: Sequence[int] | 
             p.close()
 
 
+class LunnonBatch:
+    """Many maps prepared once on the device and counted by replaying a
+    recorded CUDA graph of the batched launch (mf_lunnon_batch_*)."""
+
+    def __init__(self, shapes: Iterable[Sequence[int]], depths: Sequence[int] | None = None,
+                 cfg=None):
+        lib = _native.load()
+        self.shapes = [tuple(s) for s in shapes]
+        plans = [LunnonPlan(s) for s in self.shapes]
+        try:
+            handles = (ctypes.c_void_p * len(plans))(*[p.handle for p in plans])
+            d = None
+            if depths is not None:
+                d = (ctypes.c_int32 * len(plans))(*[int(x) for x in depths])
+            h = ctypes.c_void_p()
+            check(lib.mf_lunnon_batch_create(handles, len(plans), d, _cfg(cfg), ctypes.byref(h)))
+            self._h = h
+        finally:
+            for p in plans:
+                p.close()
+
+    def run(self):
+        """(per-map counts, RunStats) -- one graph replay."""
+        out = (ctypes.c_uint64 * len(self.shapes))()
+        st = RunStats()
+        check(_native.load().mf_lunnon_batch_run(self._h, out, ctypes.byref(st)))
+        return [int(v) for v in out], st
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _native.load().mf_lunnon_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SymGraph:
+    """A batched sym count on fixed device buffers, recorded once as a CUDA
+    graph and replayed with launch() (mf_sym_graph_*)."""
+
+    def __init__(self, n: int, start_i: int, stop_i: int, d_cycles: int, num: int,
+                 d_counts: int, d_workspace: int, workspace_bytes: int, d_nodes: int = 0,
+                 cfg=None):
+        h = ctypes.c_void_p()
+        check(_native.load().mf_sym_graph_create(n, start_i, stop_i, d_cycles or None, num,
+                                                 d_counts or None, d_nodes or None,
+                                                 d_workspace or None, workspace_bytes,
+                                                 _cfg(cfg), ctypes.byref(h)))
+        self._h = h
+
+    def launch(self, stream: int = 0) -> None:
+        check(_native.load().mf_graph_launch(self._h, stream or None))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _native.load().mf_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def sym_edges(n: int) -> np.ndarray:
     out = np.zeros((4, 64), np.uint8)
     check(_native.load().mf_sym_edges(n, out.ctypes.data))
@@ -274,7 +343,8 @@ def solve_cases(n: int, start_i: int, stop_i: int, case_buffer: bytes, case_coun
 
 
 __all__ = [
-    "BatchConfig", "EngineError", "RunStats", "LunnonPlan", "SymPlan", "gpu_folding",
+    "BatchConfig", "EngineError", "RunStats", "LunnonPlan", "LunnonBatch", "SymPlan", "SymGraph",
+    "gpu_folding",
     "lunnon_batch_count", "sym_edges", "sym_fold", "count_cases_device", "sym_workspace_bytes",
     "count_cases_batched_device", "pack_case_buffer", "solve_cases",
 ]

@@ -433,6 +433,264 @@ int32_t mf_lunnon_batch_count(const mf_lunnon_plan *const *plans, int32_t num_pl
     return lunnon_batch_impl(plans, num_plans, depths, nullptr, nullptr, cfg, counts_out, stats);
 }
 
+}  // extern "C"
+
+// ------------------------------------------------------- graph replay ----
+
+struct mf_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+// Record what `body` enqueues on a private stream into an instantiated graph.
+template <class F>
+int capture_graph(F &&body, mf_graph **out) {
+    cudaStream_t s = nullptr;
+    MF_TRY_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(s);
+        set_error("cudaStreamBeginCapture failed: %s", cudaGetErrorString(e));
+        return MF_ERR_CUDA;
+    }
+    const cudaError_t eb = body(s);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(s, &g);
+    cudaStreamDestroy(s);
+    if (eb != cudaSuccess || ee != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        set_error("recording the launch failed: %s",
+                  cudaGetErrorString(eb != cudaSuccess ? eb : ee));
+        return MF_ERR_CUDA;
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, g, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        set_error("cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
+        return MF_ERR_CUDA;
+    }
+    auto *gr = new mf_graph;
+    gr->graph = g;
+    gr->exec = exec;
+    *out = gr;
+    return MF_OK;
+}
+
+}  // namespace
+
+struct mf_lunnon_batch {
+    int num_plans = 0;
+    uint64_t units = 0;
+    uint64_t h2d_bytes = 0;
+    uint8_t *d_units = nullptr;
+    uint8_t *d_meta = nullptr;
+    uint64_t *d_counts = nullptr;  // num_plans counts + node counter
+    void *d_work = nullptr;
+    uint64_t *h_out = nullptr;     // pinned: counts + node counter + queue header
+    mf_graph *graph = nullptr;
+    cudaStream_t stream = nullptr;
+};
+
+extern "C" {
+
+static int check_sym_range(int32_t n, int32_t start_i, int32_t stop_i);
+
+int32_t mf_sym_graph_create(int32_t n, int32_t start_i, int32_t stop_i, const uint8_t *d_cycles,
+                            uint64_t num_cases, uint64_t *d_counts, uint64_t *d_nodes,
+                            void *d_workspace, uint64_t workspace_bytes_,
+                            const mf_batch_config *cfg, mf_graph **out) {
+    clear_error();
+    if (!out) {
+        set_error("out is NULL");
+        return MF_ERR_ARG;
+    }
+    *out = nullptr;
+    int rc = check_sym_range(n, start_i, stop_i);
+    if (rc) return rc;
+    const BatchKnobs knobs = resolve_knobs(cfg);
+    if (!d_workspace || workspace_bytes_ < workspace_bytes(knobs.queue_capacity)) {
+        set_error("workspace must hold %llu bytes",
+                  (unsigned long long)workspace_bytes(knobs.queue_capacity));
+        return MF_ERR_CAPACITY;
+    }
+    if (num_cases && (!d_cycles || !d_counts)) {
+        set_error("d_cycles and d_counts are required");
+        return MF_ERR_ARG;
+    }
+    if (reinterpret_cast<uintptr_t>(d_cycles) % 16 || reinterpret_cast<uintptr_t>(d_workspace) % 256) {
+        set_error("d_cycles must be 16-byte and d_workspace 256-byte aligned");
+        return MF_ERR_ARG;
+    }
+    const uint8_t *edges = device_edges(n);
+    if (!edges) {
+        set_error("uploading the edge pages failed");
+        return MF_ERR_CUDA;
+    }
+    return capture_graph(
+        [&](cudaStream_t s) -> cudaError_t {
+            if (d_nodes) {
+                cudaError_t e = cudaMemsetAsync(d_nodes, 0, sizeof(uint64_t), s);
+                if (e != cudaSuccess) return e;
+            }
+            return launch_sym_batched(edges, start_i, stop_i, d_cycles, num_cases, d_counts,
+                                      d_nodes, d_workspace, knobs, s);
+        },
+        out);
+}
+
+int32_t mf_graph_launch(mf_graph *graph, void *stream) {
+    clear_error();
+    if (!graph) {
+        set_error("graph is NULL");
+        return MF_ERR_ARG;
+    }
+    MF_TRY_CUDA(cudaGraphLaunch(graph->exec, static_cast<cudaStream_t>(stream)));
+    return MF_OK;
+}
+
+void mf_graph_destroy(mf_graph *graph) {
+    if (!graph) return;
+    if (graph->exec) cudaGraphExecDestroy(graph->exec);
+    if (graph->graph) cudaGraphDestroy(graph->graph);
+    delete graph;
+}
+
+void mf_lunnon_batch_destroy(mf_lunnon_batch *b) {
+    if (!b) return;
+    mf_graph_destroy(b->graph);
+    if (b->d_units) cudaFree(b->d_units);
+    if (b->d_meta) cudaFree(b->d_meta);
+    if (b->d_counts) cudaFree(b->d_counts);
+    if (b->d_work) cudaFree(b->d_work);
+    if (b->h_out) cudaFreeHost(b->h_out);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+int32_t mf_lunnon_batch_create(const mf_lunnon_plan *const *plans, int32_t num_plans,
+                               const int32_t *depths, const mf_batch_config *cfg,
+                               mf_lunnon_batch **out) {
+    clear_error();
+    if (!out || !plans || num_plans < 1) {
+        set_error("out, plans and num_plans >= 1 are required");
+        return MF_ERR_ARG;
+    }
+    *out = nullptr;
+    int rc = ensure_device();
+    if (rc) return rc;
+    const uint32_t stride = lunnon_state_stride(64);
+    std::vector<LunnonInstanceDev> inst(num_plans);
+    std::vector<uint8_t> meta;
+    std::vector<uint64_t> per_plan(num_plans);
+    uint64_t total = 0;
+    int max_levels = 0;
+    for (int k = 0; k < num_plans; ++k) {
+        const mf_lunnon_plan *p = plans[k];
+        if (!p) {
+            set_error("plan %d is NULL", k);
+            return MF_ERR_ARG;
+        }
+        int d = depths ? depths[k] : -1;
+        if (d < 0) d = default_lunnon_depth(p->t);
+        if (d > p->t.n) d = p->t.n;
+        inst[k] = LunnonInstanceDev{uint32_t(meta.size()), p->t.n, p->t.dim, d + 1};
+        meta.insert(meta.end(), p->t.next.begin(), p->t.next.end());
+        meta.resize((meta.size() + 15) / 16 * 16, 0);
+        per_plan[k] = collect_lunnon_states(p->t, d, nullptr, 0, stride);
+        total += per_plan[k];
+        max_levels = std::max(max_levels, p->t.n - d - 1);
+    }
+    if (meta.size() > 160 * 1024) {
+        set_error("batched maps' tables total %zu bytes; at most 163840 fit on chip", meta.size());
+        return MF_ERR_CAPACITY;
+    }
+    const uint32_t inst_offset = uint32_t(meta.size());
+    const uint8_t *ib = reinterpret_cast<const uint8_t *>(inst.data());
+    meta.insert(meta.end(), ib, ib + inst.size() * sizeof(LunnonInstanceDev));
+    const size_t unit_bytes = total * stride, owner_bytes = total * sizeof(uint32_t);
+    std::vector<uint8_t> host(unit_bytes + owner_bytes);
+    auto *owner = reinterpret_cast<uint32_t *>(host.data() + unit_bytes);
+    uint64_t at = 0;
+    for (int k = 0; k < num_plans; ++k) {
+        collect_lunnon_states(plans[k]->t, inst[k].start_leaf - 1, host.data() + at * stride,
+                              per_plan[k], stride);
+        for (uint64_t s = 0; s < per_plan[k]; ++s) owner[at + s] = uint32_t(k);
+        at += per_plan[k];
+    }
+    auto b = std::unique_ptr<mf_lunnon_batch, void (*)(mf_lunnon_batch *)>(new mf_lunnon_batch,
+                                                                           mf_lunnon_batch_destroy);
+    b->num_plans = num_plans;
+    b->units = total;
+    b->h2d_bytes = host.size() + meta.size();
+    const BatchKnobs knobs = resolve_knobs(cfg);
+    MF_TRY_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    MF_TRY_CUDA(cudaMalloc(&b->d_units, std::max<size_t>(host.size(), 16)));
+    MF_TRY_CUDA(cudaMalloc(&b->d_meta, (meta.size() + 255) / 256 * 256));
+    MF_TRY_CUDA(cudaMalloc(&b->d_counts, (num_plans + 1) * sizeof(uint64_t)));
+    MF_TRY_CUDA(cudaMalloc(&b->d_work, workspace_bytes(knobs.queue_capacity)));
+    MF_TRY_CUDA(cudaMallocHost(&b->h_out, (num_plans + 1) * sizeof(uint64_t) + sizeof(QueueHeader)));
+    MF_TRY_CUDA(cudaMemcpy(b->d_units, host.data(), host.size(), cudaMemcpyHostToDevice));
+    MF_TRY_CUDA(cudaMemcpy(b->d_meta, meta.data(), meta.size(), cudaMemcpyHostToDevice));
+    mf_lunnon_batch *raw = b.get();
+    rc = capture_graph(
+        [&](cudaStream_t s) -> cudaError_t {
+            cudaError_t e = cudaMemsetAsync(raw->d_counts + num_plans, 0, sizeof(uint64_t), s);
+            if (e != cudaSuccess) return e;
+            return launch_lunnon_batched(raw->d_meta, uint32_t(meta.size()), inst_offset, num_plans,
+                                         max_levels, raw->d_units,
+                                         reinterpret_cast<uint32_t *>(raw->d_units + unit_bytes),
+                                         total, raw->d_counts, raw->d_counts + num_plans,
+                                         raw->d_work, knobs, s);
+        },
+        &b->graph);
+    if (rc) return rc;
+    *out = b.release();
+    return MF_OK;
+}
+
+int32_t mf_lunnon_batch_run(mf_lunnon_batch *b, uint64_t *counts_out, mf_run_stats *stats) {
+    clear_error();
+    if (!b || !counts_out) {
+        set_error("batch and counts_out are required");
+        return MF_ERR_ARG;
+    }
+    const double t0 = now_seconds();
+    const int np = b->num_plans;
+    Timer tk, td;
+    cudaEventRecord(tk.a, b->stream);
+    MF_TRY_CUDA(cudaGraphLaunch(b->graph->exec, b->stream));
+    cudaEventRecord(tk.b, b->stream);
+    cudaEventRecord(td.a, b->stream);
+    MF_TRY_CUDA(cudaMemcpyAsync(b->h_out, b->d_counts, (np + 1) * sizeof(uint64_t),
+                                cudaMemcpyDeviceToHost, b->stream));
+    MF_TRY_CUDA(cudaMemcpyAsync(b->h_out + np + 1, b->d_work, sizeof(QueueHeader),
+                                cudaMemcpyDeviceToHost, b->stream));
+    cudaEventRecord(td.b, b->stream);
+    MF_TRY_CUDA(cudaStreamSynchronize(b->stream));
+    const QueueHeader *hdr = reinterpret_cast<const QueueHeader *>(b->h_out + np + 1);
+    if (hdr->error) {
+        set_error("batched kernel saw a malformed prefix state");
+        return MF_ERR_TIMEOUT;
+    }
+    for (int k = 0; k < np; ++k) counts_out[k] = b->h_out[k];
+    if (stats) {
+        *stats = mf_run_stats{};
+        stats->kernel_s = tk.seconds();
+        stats->d2h_s = td.seconds();
+        stats->total_s = now_seconds() - t0;
+        stats->units = b->units;
+        stats->nodes = b->h_out[np];
+        stats->tasks = hdr->tasks_run;
+        stats->splits = hdr->spawn_tail;
+        stats->h2d_bytes = 0;
+        stats->d2h_bytes = (np + 1) * sizeof(uint64_t) + sizeof(QueueHeader);
+    }
+    return MF_OK;
+}
+
 // ---------------------------------------------------------------- sym ----
 
 int32_t mf_sym_edges(int32_t n, uint8_t *out) {

@@ -26,6 +26,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "engine.hpp"
 
@@ -870,15 +871,41 @@ int pick_levels(int levels, bool local = false) {
     return 0;
 }
 
+// Raise the kernel's dynamic shared-memory limit and size its persistent
+// grid from the occupancy calculator.  Results are cached per (device,
+// kernel, shared bytes), so a launch recorded into a CUDA graph makes no
+// attribute or occupancy calls.
+struct FitEntry {
+    int dev;
+    const void *fn;
+    size_t smem;
+    int fit;
+};
+std::mutex g_fit_mu;
+FitEntry g_fit[256];
+int g_fit_len = 0;
+
 template <class K>
 cudaError_t prepare(K kernel, size_t smem, int tpb, int want_per_sm, int &blocks_per_sm) {
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(smem));
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
+    const void *fn = reinterpret_cast<const void *>(kernel);
     int fit = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kernel, tpb, smem);
-    if (e != cudaSuccess) return e;
-    if (fit < 1) return cudaErrorInvalidConfiguration;
+    {
+        std::lock_guard<std::mutex> lock(g_fit_mu);
+        for (int k = 0; k < g_fit_len; ++k)
+            if (g_fit[k].dev == dev && g_fit[k].fn == fn && g_fit[k].smem == smem) fit = g_fit[k].fit;
+    }
+    if (fit == 0) {
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kernel, tpb, smem);
+        if (e != cudaSuccess) return e;
+        if (fit < 1) return cudaErrorInvalidConfiguration;
+        std::lock_guard<std::mutex> lock(g_fit_mu);
+        if (g_fit_len < 256) g_fit[g_fit_len++] = FitEntry{dev, fn, smem, fit};
+    }
     blocks_per_sm = want_per_sm > 0 && want_per_sm < fit ? want_per_sm : fit;
     return cudaSuccess;
 }
