@@ -871,18 +871,20 @@ int pick_levels(int levels, bool local = false) {
     return 0;
 }
 
-// Raise the kernel's dynamic shared-memory limit and size its persistent
-// grid from the occupancy calculator.  Results are cached per (device,
+// Size a kernel's persistent grid from the occupancy calculator.  The first
+// time a kernel is seen on a device its dynamic shared-memory limit is raised
+// once to the device's opt-in maximum (never lowered again, so every later
+// launch size stays legal); occupancy results are cached per (device,
 // kernel, shared bytes), so a launch recorded into a CUDA graph makes no
 // attribute or occupancy calls.
 struct FitEntry {
     int dev;
     const void *fn;
-    size_t smem;
+    size_t smem;  // 0: the kernel's shared-memory limit has been raised
     int fit;
 };
 std::mutex g_fit_mu;
-FitEntry g_fit[256];
+FitEntry g_fit[512];
 int g_fit_len = 0;
 
 template <class K>
@@ -892,19 +894,30 @@ cudaError_t prepare(K kernel, size_t smem, int tpb, int want_per_sm, int &blocks
     if (e != cudaSuccess) return e;
     const void *fn = reinterpret_cast<const void *>(kernel);
     int fit = 0;
+    bool raised = false;
     {
         std::lock_guard<std::mutex> lock(g_fit_mu);
-        for (int k = 0; k < g_fit_len; ++k)
-            if (g_fit[k].dev == dev && g_fit[k].fn == fn && g_fit[k].smem == smem) fit = g_fit[k].fit;
+        for (int k = 0; k < g_fit_len; ++k) {
+            if (g_fit[k].dev != dev || g_fit[k].fn != fn) continue;
+            if (g_fit[k].smem == 0) raised = true;
+            else if (g_fit[k].smem == smem) fit = g_fit[k].fit;
+        }
+    }
+    if (!raised) {
+        int optin = 0;
+        e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        if (e != cudaSuccess) return e;
+        std::lock_guard<std::mutex> lock(g_fit_mu);
+        if (g_fit_len < 512) g_fit[g_fit_len++] = FitEntry{dev, fn, 0, 0};
     }
     if (fit == 0) {
-        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        if (e != cudaSuccess) return e;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kernel, tpb, smem);
         if (e != cudaSuccess) return e;
         if (fit < 1) return cudaErrorInvalidConfiguration;
         std::lock_guard<std::mutex> lock(g_fit_mu);
-        if (g_fit_len < 256) g_fit[g_fit_len++] = FitEntry{dev, fn, smem, fit};
+        if (g_fit_len < 512) g_fit[g_fit_len++] = FitEntry{dev, fn, smem, fit};
     }
     blocks_per_sm = want_per_sm > 0 && want_per_sm < fit ? want_per_sm : fit;
     return cudaSuccess;
