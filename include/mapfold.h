@@ -199,6 +199,28 @@ int32_t mf_sym_plan_solve(const mf_sym_plan *plan, uint64_t max_cases, uint64_t 
                           int32_t mode, const mf_batch_config *cfg, uint64_t *answer_lo_hi,
                           mf_run_stats *stats);
 
+/* Allocation-free variant of mf_sym_count_cases_batched.  No counterpart in
+ * the reference.  It is for callers that cannot allocate device memory at
+ * all and therefore cannot pass a workspace: a process whose GPU memory is
+ * owned by another allocator (a framework's caching pool that has reserved
+ * the device), or a latency-critical caller that must not take the implicit
+ * device synchronisation of cudaMalloc/cudaFree.  The split-item ring lives
+ * in a fixed __device__ array of 4096 cells (416.25 KiB, plus 2.25 KiB of
+ * edge pages) that every GPU loading this library holds until the process
+ * exits; a cfg->queue_capacity above 4096 is rejected with MF_ERR_CAPACITY.
+ * The caller still passes inputs and outputs (d_cycles, d_counts, d_nodes).
+ * The first call on a device performs its one-time set-up (looks up the
+ * array's device address and copies the edge pages in), so make that first
+ * call before any stream capture.  All calls share the array and it keeps the
+ * last call's contents; each call clears what must start at zero, but calls
+ * that overlap on the GPU (concurrent streams, other host threads) race on it
+ * and must be serialised by the caller.  It calls no cudaMalloc, cudaFree or
+ * other allocating routine. */
+int32_t mf_sym_count_cases_batched_static(int32_t n, int32_t start_i, int32_t stop_i,
+                                          const uint8_t *d_cycles, uint64_t num_cases,
+                                          uint64_t *d_counts, uint64_t *d_nodes,
+                                          const mf_batch_config *cfg, void *stream);
+
 /* ---- CUDA-graph replay ------------------------------------------------ */
 
 typedef struct mf_graph mf_graph;

@@ -1110,3 +1110,104 @@ cudaError_t launch_lunnon_batched(const uint8_t *d_meta, uint32_t meta_bytes, ui
 }
 
 }  // namespace mf
+
+// ------------------------------------------- allocation-free entry point --
+//
+// mf_sym_count_cases_batched_static: the batched sym kernel with its split
+// ring in a fixed device array instead of a caller-provided workspace.  For
+// callers that cannot allocate device memory at all -- a process whose HBM is
+// owned by another allocator, or a latency-critical caller that must not hit
+// the implicit device synchronisation of cudaMalloc/cudaFree -- and therefore
+// cannot hand over a workspace either.  Every GPU that loads this library
+// holds these arrays until the process exits.
+
+namespace mf {
+namespace {
+
+constexpr uint64_t kStaticRingCells = 4096;  // split-ring cells (power of two)
+constexpr size_t kStaticWorkspaceBytes =
+    256 + kStaticRingCells * (sizeof(TaskRecord) + sizeof(unsigned long long));  // 416.25 KiB
+
+__device__ __align__(256) uint8_t g_static_workspace[kStaticWorkspaceBytes];
+__device__ __align__(256) uint8_t g_static_edges[9][4 * kSymCells];  // edge pages per n
+
+struct StaticState {
+    bool ready = false;
+    void *workspace = nullptr;
+    uint8_t *edges = nullptr;
+};
+
+std::mutex g_static_mu;
+StaticState g_static[64];
+
+// Once per device, with that device current: look up the arrays' device
+// addresses (a host-side name of a __device__ array is not a device address)
+// and fill the edge pages of every board size.
+int static_setup(int dev, StaticState *&out) {
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    StaticState &s = g_static[dev];
+    if (!s.ready) {
+        void *ws = nullptr, *edges = nullptr;
+        MF_TRY_CUDA(cudaGetSymbolAddress(&ws, g_static_workspace));
+        MF_TRY_CUDA(cudaGetSymbolAddress(&edges, g_static_edges));
+        uint8_t host[9][4 * kSymCells] = {};
+        for (int n = 2; n <= 8; ++n) sym_edges(n, host[n]);
+        MF_TRY_CUDA(cudaMemcpy(edges, host, sizeof(host), cudaMemcpyHostToDevice));
+        s.workspace = ws;
+        s.edges = static_cast<uint8_t *>(edges);
+        s.ready = true;
+    }
+    out = &s;
+    return MF_OK;
+}
+
+}  // namespace
+}  // namespace mf
+
+extern "C" int32_t mf_sym_count_cases_batched_static(int32_t n, int32_t start_i, int32_t stop_i,
+                                                     const uint8_t *d_cycles, uint64_t num_cases,
+                                                     uint64_t *d_counts, uint64_t *d_nodes,
+                                                     const mf_batch_config *cfg, void *stream) {
+    using namespace mf;
+    clear_error();
+    if (n < 2 || n > 8) {
+        set_error("n must be between 2 and 8");
+        return MF_ERR_ARG;
+    }
+    if (start_i < 0 || start_i > stop_i || stop_i > n * n) {
+        set_error("need 0 <= start_i <= stop_i <= n*n");
+        return MF_ERR_RANGE;
+    }
+    if (cfg && cfg->queue_capacity > kStaticRingCells) {
+        set_error("queue_capacity %llu exceeds the fixed split ring of %llu cells",
+                  (unsigned long long)cfg->queue_capacity, (unsigned long long)kStaticRingCells);
+        return MF_ERR_CAPACITY;
+    }
+    if (num_cases > 0xffffffffULL) {
+        set_error("at most 2^32-1 cases per call");
+        return MF_ERR_ARG;
+    }
+    if (num_cases && (!d_cycles || !d_counts)) {
+        set_error("d_cycles and d_counts are required");
+        return MF_ERR_ARG;
+    }
+    if (reinterpret_cast<uintptr_t>(d_cycles) % 16) {
+        set_error("d_cycles must be 16-byte aligned");
+        return MF_ERR_ARG;
+    }
+    int dev = 0;
+    MF_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_error("device ordinal %d out of range", dev);
+        return MF_ERR_ARG;
+    }
+    StaticState *s = nullptr;
+    int rc = static_setup(dev, s);
+    if (rc) return rc;
+    BatchKnobs knobs = resolve_knobs(cfg);
+    knobs.queue_capacity = kStaticRingCells;
+    MF_TRY_CUDA(launch_sym_batched(s->edges + size_t(n) * 4 * kSymCells, start_i, stop_i, d_cycles,
+                                   num_cases, d_counts, d_nodes, s->workspace, knobs,
+                                   static_cast<cudaStream_t>(stream)));
+    return MF_OK;
+}
