@@ -250,6 +250,54 @@ int32_t mf_lunnon_batch_create(const mf_lunnon_plan *const *plans, int32_t num_p
 int32_t mf_lunnon_batch_run(mf_lunnon_batch *batch, uint64_t *counts_out, mf_run_stats *stats);
 void mf_lunnon_batch_destroy(mf_lunnon_batch *batch);
 
+/* ======================================================================
+ * Request server: continuous batching on one resident kernel
+ * ====================================================================== */
+
+typedef struct mf_server mf_server;
+
+typedef struct {
+    uint64_t unit_capacity;  /* device unit arena, in units (power of 2; 0: 2^21) */
+    uint32_t max_requests;   /* requests resident at once (0: 1024) */
+    uint32_t block_threads;  /* 0: 128 */
+    uint64_t table_bytes;    /* Lunnon neighbour-table arena (0: 64 MiB) */
+    uint32_t node_budget;    /* rounds between split checks (0: 64) */
+    uint32_t reserved;
+    uint64_t queue_capacity; /* split-item ring cells (0: 2^16) */
+} mf_server_config;
+
+typedef struct {
+    double submit_s;  /* monotonic clock at submission */
+    double admit_s;   /* ... when its units were resident and published */
+    double done_s;    /* ... when the server saw its result */
+    uint64_t units;   /* cases or prefix states */
+    uint64_t nodes;   /* reference nodes searched for it */
+} mf_request_info;
+
+/* Starts a server on the current device: a persistent kernel that keeps
+ * running while requests come and go.  A request is admitted as soon as a
+ * slot and enough unit-arena memory are free; its units then start on
+ * whichever lanes free up first, alongside the requests already running,
+ * and its subtrees share the one split-item ring.  No reference counterpart:
+ * the reference runs one chunk per process or container (modal_sym.py:88-137). */
+int32_t mf_server_create(const mf_server_config *cfg, mf_server **out);
+/* Submit sym_fold cases [start_case, start_case + max_cases) of an n x n
+ * map at MF_EXPANDED_N = expanded_n; the result is what `sym_fold` prints
+ * for that chunk.  Returns at once with a request id. */
+int32_t mf_server_submit_sym(mf_server *srv, int32_t n, int32_t expanded_n, uint64_t start_case,
+                             uint64_t max_cases, uint64_t *request_id);
+/* Submit a whole-map Lunnon count (depth < 0: default split depth). */
+int32_t mf_server_submit_lunnon(mf_server *srv, const int32_t *dims, int32_t ndim, int32_t depth,
+                                uint64_t *request_id);
+/* *done = 1 and the answer (lo, hi) once the request has finished. */
+int32_t mf_server_poll(mf_server *srv, uint64_t request_id, int32_t *done, uint64_t *answer_lo_hi,
+                       mf_request_info *info);
+/* Blocks until the request finishes or timeout_s passes (MF_ERR_TIMEOUT). */
+int32_t mf_server_wait(mf_server *srv, uint64_t request_id, double timeout_s,
+                       uint64_t *answer_lo_hi, mf_request_info *info);
+/* Finishes outstanding requests, stops the kernel, frees everything. */
+void mf_server_destroy(mf_server *srv);
+
 /* The whole `sym_fold n threads max_cases start_case` computation with the
  * MF_EXPANDED_N semantics: answer = n*n * sum(multiplier * count) over the
  * selected cases (n <= 5: 2*n*n*count).  mode 0 = plain kernel, 1 =

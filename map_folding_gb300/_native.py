@@ -57,6 +57,28 @@ class BatchConfig(ctypes.Structure):
     ]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [
+        ("unit_capacity", ctypes.c_uint64),
+        ("max_requests", ctypes.c_uint32),
+        ("block_threads", ctypes.c_uint32),
+        ("table_bytes", ctypes.c_uint64),
+        ("node_budget", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+        ("queue_capacity", ctypes.c_uint64),
+    ]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [
+        ("submit_s", ctypes.c_double),
+        ("admit_s", ctypes.c_double),
+        ("done_s", ctypes.c_double),
+        ("units", ctypes.c_uint64),
+        ("nodes", ctypes.c_uint64),
+    ]
+
+
 class EngineError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"mapfold status {status}: {message}")
@@ -93,6 +115,12 @@ SIGNATURES = {
     "mf_lunnon_batch_create": ([_p, _i32, _p, _p, ctypes.POINTER(_p)], _i32),
     "mf_lunnon_batch_run": ([_p, _p, _p], _i32),
     "mf_lunnon_batch_destroy": ([_p], None),
+    "mf_server_create": ([_p, ctypes.POINTER(_p)], _i32),
+    "mf_server_submit_sym": ([_p, _i32, _i32, _u64, _u64, _pu64], _i32),
+    "mf_server_submit_lunnon": ([_p, _p, _i32, _i32, _pu64], _i32),
+    "mf_server_poll": ([_p, _u64, ctypes.POINTER(_i32), _p, _p], _i32),
+    "mf_server_wait": ([_p, _u64, ctypes.c_double, _p, _p], _i32),
+    "mf_server_destroy": ([_p], None),
     "mf_sym_solve": ([_i32, _u64, _u64, _i32, _i32, _p, _p, _p], _i32),
     "mf_solve_cases": ([_u32, _u32, _u32, _p, _u32, _p], _u32),
 }

@@ -25,7 +25,7 @@ BIN = PKG / "bin"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include")]
-LIB_SOURCES = ["host.cpp", "capi.cpp", "dfs_kernels.cu"]
+LIB_SOURCES = ["host.cpp", "capi.cpp", "dfs_kernels.cu", "serve.cu"]
 CLI_SOURCES = {"gpu_folding": "cli_gpu_folding.cpp", "gpu_folding_v2": "cli_gpu_folding_v2.cpp",
                "sym_fold": "cli_sym_fold.cpp"}
 
@@ -53,7 +53,8 @@ def _stale(target: Path, deps: list[Path]) -> bool:
 def build(force: bool = False, verbose: bool = False) -> Path:
     OBJ.mkdir(exist_ok=True)
     BIN.mkdir(exist_ok=True)
-    headers = sorted(CSRC.glob("*.hpp")) + sorted(CSRC.glob("*.inl")) + [ROOT / "include" / "mapfold.h"]
+    headers = (sorted(CSRC.glob("*.hpp")) + sorted(CSRC.glob("*.inl")) + sorted(CSRC.glob("*.cuh"))
+               + [ROOT / "include" / "mapfold.h"])
     cc = nvcc()
     jobs = []
     objs = []

@@ -729,6 +729,23 @@ int32_t mf_sym_plan_create(int32_t n, int32_t expanded_n, mf_sym_plan **out) {
 
 void mf_sym_plan_destroy(mf_sym_plan *plan) { delete plan; }
 
+}  // extern "C"
+
+namespace mf {
+int build_full_sym_plan(int n, int expanded_n, SymPlan &plan) {
+    std::string why;
+    int rc = build_sym_plan(n, expanded_n, plan, why);
+    if (rc) {
+        set_error("%s", why.c_str());
+        return rc;
+    }
+    if (plan.mid_first.empty()) return complete_index(plan);
+    return MF_OK;
+}
+}  // namespace mf
+
+extern "C" {
+
 int32_t mf_sym_plan_info(const mf_sym_plan *plan, int32_t *n, int32_t *start_i,
                          uint64_t *center_cases, uint64_t *reduced_cases, uint64_t *total_cases) {
     clear_error();

@@ -28,342 +28,13 @@
 #include <cstring>
 #include <mutex>
 
+#include "dfs_core.cuh"
 #include "engine.hpp"
 
 namespace mf {
 namespace {
 
-constexpr unsigned kFull = 0xffffffffu;
-constexpr int kLocalLevels = 66;    // local-memory stack: levels 0..65
-constexpr int kMinSplitHeight = 4;  // never hand out subtrees shallower than this
-
-__device__ __forceinline__ uint64_t low_bits(int k) {
-    return k >= 64 ? ~0ULL : ((1ULL << k) - 1ULL);
-}
-
-// Per-thread byte array in shared memory.  Byte j of thread t lives in
-// 32-bit word (j/4)*TPB + t, so a warp's 32 lanes always address 32
-// different banks, whatever indices they touch.
-template <int TPB>
-struct List {
-    uint8_t *base;  // smem + 4 * threadIdx.x
-    __device__ __forceinline__ int get(int j) const { return base[(j & ~3) * TPB + (j & 3)]; }
-    __device__ __forceinline__ void put(int j, int v) const {
-        base[(j & ~3) * TPB + (j & 3)] = static_cast<uint8_t>(v);
-    }
-    __device__ __forceinline__ uint32_t word(int w) const {
-        return reinterpret_cast<const uint32_t *>(base)[w * TPB];
-    }
-    __device__ __forceinline__ void set_word(int w, uint32_t v) const {
-        reinterpret_cast<uint32_t *>(base)[w * TPB] = v;
-    }
-};
-
-// A unit's list is usable only if it is a permutation of the placed items
-// (items >= placed are written before they are read).  That is also what
-// makes every walk below terminate without a step bound: each walk iterates
-// an injective map (the list composed with an involution -- the page's
-// partner matching for sym, the dimension's neighbour table d[l][.] for
-// Lunnon) from a point with no preimage, so it reaches its end in fewer
-// than `placed` + 1 steps.  Insertions keep the list a permutation.
-template <int TPB>
-__device__ __forceinline__ bool list_valid(const List<TPB> &L, int placed) {
-    bool ok = true;
-    uint64_t seen_lo = 0, seen_hi = 0;
-    for (int k = 0; k < placed; ++k) {
-        const int v = L.get(k);
-        ok &= v < placed;
-        if (v < 64) seen_lo |= 1ULL << v;
-        else seen_hi |= 1ULL << (v & 63);
-    }
-    const uint64_t want_lo = low_bits(placed);
-    const uint64_t want_hi = placed > 64 ? low_bits(placed - 64) : 0;
-    return ok && seen_lo == want_lo && seen_hi == want_hi;
-}
-
-// ------------------------------------------------------------- rules -----
-
-// sym_fold.cpp:179-204: positions j < i after which cell i may follow in the
-// stack.  For each edge page whose neighbour `other` of i is placed, walk the
-// cycle from `other`, hopping over every placed partner pair, and keep the
-// positions landed on; AND the pages.  The pages' walks run as one flat loop
-// (a lane moves on to its next page inside the same loop), so a warp waits
-// for its longest lane's total walk, not for the sum of per-page maxima.
-struct SymRules {
-    const uint8_t *edge;  // 4 pages x 64, shared memory
-    const uint32_t *nb4;  // per cell: its 4 page neighbours, one byte each
-    template <int TPB>
-    __device__ __forceinline__ uint64_t gaps(const List<TPB> &L, int i,
-                                             unsigned long long &nodes) const {
-        ++nodes;
-        uint64_t good = low_bits(i);
-        // Pages whose neighbour of i is placed: one word, four byte compares.
-        const uint32_t nb = nb4[i];
-        const uint32_t placed = __vcmpltu4(nb, 0x01010101u * uint32_t(i)) & 0x01010101u;
-        unsigned pend = (placed * 0x01020408u) >> 24;
-        const uint8_t *e = edge;
-        uint64_t allowed = ~0ULL;
-        int other = 0, j = 0;
-        for (;;) {
-            if (j == other) {  // current page finished (or none started)
-                good &= allowed;
-                if (!good || !pend) break;
-                const int p = __ffs(pend) - 1;
-                pend &= pend - 1;
-                e = edge + p * kSymCells;
-                other = (nb >> (8 * p)) & 0xff;
-                allowed = 1ULL << other;
-                j = L.get(other);
-                continue;
-            }
-            const int partner = e[j];
-            j = partner < i ? partner : j;
-            allowed |= 1ULL << j;
-            j = L.get(j);
-        }
-        return good;
-    }
-};
-
-// mf.c:88-124 with the gap stack replaced by masks: for every constrained
-// dimension walk m = d[l][l], d[l][b[m]], ... up to l and collect the walked
-// positions; a gap is a position every constrained dimension walked (the
-// reference's count[m] == dim - dd); with no constrained dimension every
-// position 0..l-1 is a gap.  Position 0 (insert on top of the sentinel) is
-// dropped for l >= 2: it makes b[0] = l != 1 and the normal-form filter
-// (mf.c:83) would prune the whole subtree.  `nodes` counts the insertions
-// the reference loop would make (mf.c:136-142), position 0 included.  As for
-// sym, the dimensions' walks run as one flat loop.
-struct LunnonRules {
-    const uint8_t *table;  // [dim][n+1][n+1]
-    int n;
-    int dim;
-    template <int TPB>
-    __device__ __forceinline__ uint64_t gaps(const List<TPB> &L, int l,
-                                             unsigned long long &nodes) const {
-        const int w = n + 1;
-        uint64_t mask = ~0ULL, walked = ~0ULL;
-        int bound = 0, d = -1, m = l;
-        const uint8_t *row = table;
-        for (;;) {
-            if (m == l) {  // current dimension finished (or none started)
-                mask &= walked;
-                if (!mask) break;
-                int first = l;
-                while (++d < dim) {
-                    row = table + (d * w + l) * w;
-                    first = row[l];
-                    if (first != l) break;
-                }
-                if (d >= dim) break;
-                ++bound;
-                m = first;
-                walked = 0;
-                continue;
-            }
-            walked |= 1ULL << m;
-            m = row[L.get(m)];
-        }
-        if (!bound) mask = low_bits(l);
-        nodes += __popcll(mask);
-        if (l >= 2) mask &= ~1ULL;
-        return mask;
-    }
-};
-
-// ------------------------------------------------------------- stacks ----
-
-// Per-level search state: the untried positions (mask) and the position the
-// level's item was inserted after (chosen).  Levels are stored relative to
-// `base`, the unit's first level.
-template <int TPB, int LEVELS>
-struct SmemStack {
-    static constexpr int kLevels = LEVELS;
-    uint64_t *mask;  // &s_mask[threadIdx.x], level k at mask[k * TPB]
-    List<TPB> chosen;
-    int base;
-    __device__ __forceinline__ uint64_t get(int lvl) const { return mask[(lvl - base) * TPB]; }
-    __device__ __forceinline__ void set(int lvl, uint64_t v) const { mask[(lvl - base) * TPB] = v; }
-    __device__ __forceinline__ int pick(int lvl) const { return chosen.get(lvl - base); }
-    __device__ __forceinline__ void set_pick(int lvl, int j) const { chosen.put(lvl - base, j); }
-};
-
-struct LocalStack {
-    static constexpr int kLevels = kLocalLevels;
-    uint64_t mask[kLocalLevels];
-    uint8_t chosen[kLocalLevels];
-    int base;
-    __device__ __forceinline__ uint64_t get(int lvl) const { return mask[lvl - base]; }
-    __device__ __forceinline__ void set(int lvl, uint64_t v) { mask[lvl - base] = v; }
-    __device__ __forceinline__ int pick(int lvl) const { return chosen[lvl - base]; }
-    __device__ __forceinline__ void set_pick(int lvl, int j) { chosen[lvl - base] = uint8_t(j); }
-};
-
-// ---------------------------------------------------------- DFS core -----
-//
-// Lockstep form: in every round each busy lane evaluates exactly one node
-// (one gaps() call), so a warp's lanes run the expensive walk together no
-// matter where each is in its own tree.  Between evaluations a lane
-// `advance`s: it backtracks over exhausted levels and inserts its next
-// untried item, which names the level to evaluate next.
-
-// Position the lane on its next node.  Items root..lvl-1 are inserted and
-// S[lvl] holds lvl's untried positions.  Backtracks over exhausted levels,
-// inserts item lvl after the next untried position and returns lvl + 1 (the
-// level to evaluate), or -1 when the unit's subtree is exhausted.
-template <class Stk, int TPB>
-__device__ __forceinline__ int advance(const List<TPB> &L, Stk &S, int &lvl, int root) {
-    for (;;) {
-        const uint64_t cur = S.get(lvl);
-        if (cur == 0) {
-            if (lvl == root) return -1;
-            --lvl;
-            L.put(S.pick(lvl), L.get(lvl));  // detach item lvl
-            continue;
-        }
-        const int j = __ffsll(static_cast<long long>(cur)) - 1;
-        S.set(lvl, cur & (cur - 1));
-        L.put(lvl, L.get(j));  // insert item lvl after j
-        L.put(j, lvl);
-        S.set_pick(lvl, j);
-        return lvl + 1;
-    }
-}
-
-// Consume the evaluation g of level `eval`.  The last level is never
-// entered: its positions are counted and the item above it detached again.
-// Returns true when a fresh unit turns out to be finished by this round.
-template <class Stk, int TPB>
-__device__ __forceinline__ bool apply(const List<TPB> &L, Stk &S, int &lvl, int eval, int root,
-                                      int last, bool fresh, uint64_t g,
-                                      unsigned long long &leaves) {
-    if (eval == last) {
-        leaves += __popcll(g);
-        if (fresh) return true;
-        L.put(S.pick(lvl), L.get(lvl));  // detach item lvl (= eval - 1)
-        return false;
-    }
-    lvl = eval;
-    S.set(lvl, g);
-    (void)root;
-    return false;
-}
-
-template <int TPB, int WORDS>
-__device__ __forceinline__ void load_list(const List<TPB> &L, const uint8_t *__restrict__ src,
-                                          uint32_t stride) {
-    // Records are 16-byte aligned with 16-byte multiple strides: whole-vector
-    // loads, then scatter the words into the interleaved layout.
-    const uint4 *v = reinterpret_cast<const uint4 *>(src);
-    const int vecs = (stride / 16) < (WORDS + 3) / 4 ? int(stride / 16) : (WORDS + 3) / 4;
-    for (int q = 0; q < vecs; ++q) {
-        const uint4 x = __ldg(v + q);
-        const uint32_t ws[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (4 * q + k < WORDS) L.set_word(4 * q + k, ws[k]);
-    }
-    for (int w = 4 * vecs; w < WORDS; ++w) L.set_word(w, 0);
-}
-
-__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
-    return v;
-}
-
-// Shared-memory carve-up of one CTA: [tables][lists][mask stack][picks].
-template <int TPB, int WORDS, int LEVELS>
-struct Carve {
-    static constexpr size_t kList = size_t(WORDS) * 4 * TPB;
-    static constexpr size_t kMask = size_t(LEVELS) * 8 * TPB;
-    static constexpr size_t kPick = size_t((LEVELS + 3) / 4) * 4 * TPB;
-    static constexpr size_t kThreadBytes = kList + kMask + kPick;
-    __device__ static List<TPB> list(uint8_t *smem, size_t tables) {
-        return List<TPB>{smem + tables + 4 * threadIdx.x};
-    }
-    __device__ static SmemStack<TPB, LEVELS> stack(uint8_t *smem, size_t tables) {
-        SmemStack<TPB, LEVELS> s;
-        s.mask = reinterpret_cast<uint64_t *>(smem + tables + kList) + threadIdx.x;
-        s.chosen = List<TPB>{smem + tables + kList + kMask + 4 * threadIdx.x};
-        s.base = 0;
-        return s;
-    }
-};
-
-template <int TPB, int WORDS>
-struct Carve<TPB, WORDS, 0> {  // local-memory stack
-    static constexpr size_t kList = size_t(WORDS) * 4 * TPB;
-    static constexpr size_t kThreadBytes = kList;
-    __device__ static List<TPB> list(uint8_t *smem, size_t tables) {
-        return List<TPB>{smem + tables + 4 * threadIdx.x};
-    }
-};
-
-template <int TPB, int LEVELS>
-struct StackOf {
-    using type = SmemStack<TPB, LEVELS>;
-};
-template <int TPB>
-struct StackOf<TPB, 0> {
-    using type = LocalStack;
-};
-
-template <int TPB, int WORDS, int LEVELS>
-__device__ __forceinline__ void init_stack(SmemStack<TPB, LEVELS> &S, uint8_t *smem, size_t tables) {
-    S = Carve<TPB, WORDS, LEVELS>::stack(smem, tables);
-}
-template <int TPB, int WORDS, int LEVELS>
-__device__ __forceinline__ void init_stack(LocalStack &S, uint8_t *, size_t) {
-    S.base = 0;
-}
-
-// Run one loaded unit per lane to completion in lockstep rounds (no refill):
-// the plain one-thread-per-unit kernels.
-template <class Rules, class Stk, int TPB>
-__device__ __forceinline__ void run_units(const Rules &R, const List<TPB> &L, Stk &S, bool busy,
-                                          int root, int last, unsigned long long &leaves,
-                                          unsigned long long &nodes) {
-    int lvl = root, eval = root;
-    bool fresh = true;
-    if (busy && root > last) {  // nothing left to place: one completion
-        leaves += 1;
-        busy = false;
-    }
-    while (__any_sync(kFull, busy)) {
-        if (busy) {
-            const uint64_t g = R.gaps(L, eval, nodes);
-            if (apply(L, S, lvl, eval, root, last, fresh, g, leaves)) {
-                busy = false;
-            } else {
-                fresh = false;
-                eval = advance(L, S, lvl, root);
-                busy = eval >= 0;
-            }
-        }
-    }
-}
-
 // ------------------------------------------------------- plain kernels ---
-
-// Sym tables in shared memory: the 4 edge pages (256 B), then each cell's 4
-// page neighbours packed into one word (256 B).
-constexpr size_t kSymTables = 8 * kSymCells;
-
-template <int TPB>
-__device__ __forceinline__ void stage_sym_tables(uint8_t *smem, const uint8_t *__restrict__ edges) {
-    for (int k = threadIdx.x; k < 64; k += TPB) {
-        reinterpret_cast<uint32_t *>(smem)[k] = __ldg(reinterpret_cast<const uint32_t *>(edges) + k);
-        reinterpret_cast<uint32_t *>(smem + 4 * kSymCells)[k] =
-            uint32_t(__ldg(edges + k)) | (uint32_t(__ldg(edges + kSymCells + k)) << 8) |
-            (uint32_t(__ldg(edges + 2 * kSymCells + k)) << 16) |
-            (uint32_t(__ldg(edges + 3 * kSymCells + k)) << 24);
-    }
-}
-
-__device__ __forceinline__ SymRules sym_rules(const uint8_t *smem) {
-    return SymRules{smem, reinterpret_cast<const uint32_t *>(smem + 4 * kSymCells)};
-}
 
 // One thread per case: d_counts[k] = completions of case k (UINT64_MAX if
 // its cycle is malformed).  Shared memory: 4 edge pages, then the carve.
@@ -433,74 +104,6 @@ __global__ void __launch_bounds__(TPB)
 }
 
 // ------------------------------------------------- persistent kernels ----
-
-// Bounded multi-producer multi-consumer ring of split items (the sequence-
-// numbered cell scheme of D. Vyukov's bounded MPMC queue): cell c holds
-// seq == ticket when free for the producer of `ticket`, ticket + 1 once that
-// producer has published it, and ticket + capacity once its consumer has
-// copied it out.  Producers and consumers only ever claim a cell whose
-// sequence already says it is ready for them, so nobody waits on anybody.
-struct Queue {
-    QueueHeader *hdr;
-    TaskRecord *slots;
-    unsigned long long *seq;
-    unsigned long long capacity;  // power of two
-};
-
-__device__ __forceinline__ unsigned long long vload(const unsigned long long *p) {
-    return *reinterpret_cast<const volatile unsigned long long *>(p);
-}
-
-// Warp-cooperative claim of up to `want` (<= 32) consecutive tickets at the
-// ring's head (pop) or tail (push): each lane checks one cell's sequence, and
-// one CAS by lane 0 takes the run of ready cells for the whole warp, so a
-// warp makes at most one atomic per refill or donation round.  All 32 lanes
-// call it; returns the number of tickets taken (warp-uniform), the first in
-// `first`.
-__device__ __forceinline__ int ring_claim(const Queue &Q, unsigned long long *counter, int want,
-                                          bool pop, unsigned long long &first) {
-    const int lane = threadIdx.x & 31;
-    unsigned long long pos = 0;
-    if (lane == 0) pos = vload(counter);
-    pos = __shfl_sync(kFull, pos, 0);
-    const unsigned long long t = pos + lane;
-    const bool ready =
-        lane < want && vload(Q.seq + (t & (Q.capacity - 1))) == (pop ? t + 1 : t);
-    const unsigned ok = __ballot_sync(kFull, ready);
-    const int run = ok == kFull ? 32 : __ffs(~ok) - 1;  // ready cells from lane 0 on
-    int got = 0;
-    if (lane == 0 && run > 0) got = atomicCAS(counter, pos, pos + run) == pos ? run : 0;
-    first = pos;
-    return __shfl_sync(kFull, got, 0);
-}
-
-// Copy ticket t's item out and free its cell for the producer of t + capacity.
-__device__ __forceinline__ void ring_take(const Queue &Q, unsigned long long t, uint32_t (&w)[24]) {
-    const unsigned long long cell = t & (Q.capacity - 1);
-    __threadfence();
-    const uint4 *src = reinterpret_cast<const uint4 *>(Q.slots + cell);
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        const uint4 x = __ldcg(src + q);
-        w[4 * q] = x.x;
-        w[4 * q + 1] = x.y;
-        w[4 * q + 2] = x.z;
-        w[4 * q + 3] = x.w;
-    }
-    __threadfence();
-    atomicExch(Q.seq + cell, t + Q.capacity);
-}
-
-// Write ticket t's item and publish it to its consumer.
-__device__ __forceinline__ void ring_put(const Queue &Q, unsigned long long t, const uint32_t (&w)[24]) {
-    const unsigned long long cell = t & (Q.capacity - 1);
-    uint4 *dst = reinterpret_cast<uint4 *>(Q.slots + cell);
-#pragma unroll
-    for (int q = 0; q < 6; ++q)
-        __stcg(dst + q, make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]));
-    __threadfence();
-    atomicExch(Q.seq + cell, t + 1);
-}
 
 __global__ void ring_init_kernel(unsigned long long *seq, unsigned long long capacity) {
     for (unsigned long long k = blockIdx.x * blockDim.x + threadIdx.x; k < capacity;

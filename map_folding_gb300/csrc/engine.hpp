@@ -96,6 +96,10 @@ bool sym_expand(uint8_t *cycle, int from, int stop, const uint8_t *edges, F &&em
 uint64_t sym_select_cases(const SymPlan &plan, uint64_t start, uint64_t max_cases,
                           uint8_t *cycles, uint64_t *mults, uint64_t cap);
 
+// build_sym_plan plus, for deep expansions, the GPU-built case index (the
+// plan mf_sym_plan_create returns).  Returns an mf_status.
+int build_full_sym_plan(int n, int expanded_n, SymPlan &plan);
+
 // -------------------------------------------------------- device side ----
 struct BatchKnobs {
     int block_threads;
