@@ -296,6 +296,171 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def _golden_lunnon() -> dict:
+    g = json.loads((ROOT / "tests" / "golden" / "reference_counts.json").read_text())
+    counts = {k: int(v) for k, v in g["lunnon"].items()}
+    counts["6x6"] = 123912532224  # mfah/folding.py:8-17 (squares n = 1..8)
+    return counts
+
+
+def _gpu_common(args, clocks):
+    return {"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "vs_baseline": None,
+            "dtype": "u64", "clocks": clocks.summary()}
+
+
+def run_lunnon(args):
+    """Configs 1 and 2: 5x5 at depth 15, 6x6 at depth 18, every p x q map
+    with 2 <= p <= q <= 6 and the strips of 8..20 stamps; batched kernel
+    timed over `steps` runs per map (after `warmup`), the plain kernel once
+    per map; every count checked against the reference's counts."""
+    import map_folding_gb300 as mf
+
+    golden = _golden_lunnon()
+    shapes = [((5, 5), 15), ((6, 6), 18)]
+    shapes += [((p, q), -1) for p in range(2, 7) for q in range(p, 7) if (p, q) not in ((5, 5), (6, 6))]
+    shapes += [((1, n), -1) for n in range(8, 21)]
+    rows = []
+    tot_nodes = tot_b = tot_p = 0.0
+    with ClockSampler(0) as clocks:
+        for dims, depth in shapes:
+            key = "x".join(map(str, dims))
+            plan = mf.LunnonPlan(dims)
+            try:
+                for _ in range(args.warmup):
+                    plan.count(depth, "batched")
+                bt = []
+                for _ in range(args.steps):
+                    c, states, st = plan.count(depth, "batched")
+                    assert c == golden[key], (key, c)
+                    bt.append(st.kernel_s)
+                nodes = st.nodes
+                c, _, sp = plan.count(depth, "plain")
+                assert c == golden[key], (key, c)
+            finally:
+                plan.close()
+            b = sum(bt) / len(bt)
+            rows.append({"map": key, "depth": depth, "states": int(states), "nodes": int(nodes),
+                         "plain_nodes": int(sp.nodes),
+                         "batched_ms": 1e3 * b, "plain_ms": 1e3 * sp.kernel_s,
+                         "batched_vs_plain": sp.kernel_s / b})
+            tot_nodes += nodes
+            tot_b += b
+            tot_p += sp.kernel_s
+    line = {"metric": "Lunnon DFS nodes/s over configs 1-2 (5x5@15, 6x6@18, 20 rectangles, strips 8..20)",
+            "value": tot_nodes / tot_b, "unit": "nodes/s", "ms_per_step": 1e3 * tot_b,
+            "higher_is_better": True, "scaling": "weak", "data": "synthetic: exhaustive map counts",
+            "config": {"workload": "lunnon maps", "maps": len(rows)},
+            "plain_ms_per_step": 1e3 * tot_p, "batched_vs_plain": tot_p / tot_b,
+            "maps": rows, "gpu_launches": 2 * len(rows) * args.steps}
+    line.update(_gpu_common(args, clocks))
+    print(json.dumps(line), flush=True)
+
+
+def run_uneven(args, seed: int = 2026):
+    """Config 3: 64 maps drawn from a seed, all their prefix states in one
+    persistent launch replayed from a CUDA graph, with depths and launch
+    knobs from the autotuner; compared with the plain kernel map by map."""
+    import map_folding_gb300 as mf
+    from map_folding_gb300 import autotune
+    from map_folding_gb300.workloads import uneven_instances
+
+    shapes = uneven_instances(seed, 64)
+    tuned = autotune.tune_lunnon_batch(shapes)
+    batch = mf.LunnonBatch(shapes, tuned["depths"], autotune.as_config(tuned))
+    try:
+        for _ in range(args.warmup):
+            batch.run()
+        times = []
+        with ClockSampler(0) as clocks:
+            for _ in range(args.steps):
+                counts, st = batch.run()
+                times.append(st.kernel_s)
+        nodes = st.nodes
+    finally:
+        batch.close()
+    plain = []
+    plain_s = 0.0
+    for dims, depth in zip(shapes, tuned["depths"]):
+        plan = mf.LunnonPlan(dims)
+        try:
+            c, _, sp = plan.count(depth, "plain")
+        finally:
+            plan.close()
+        plain.append(c)
+        plain_s += sp.kernel_s
+    assert counts == plain, "batched counts differ from the plain kernel"
+    golden = _golden_lunnon()
+    for dims, c in zip(shapes, counts):
+        key = "x".join(map(str, dims))
+        if key in golden:
+            assert c == golden[key], (key, c)
+    t = sum(times) / len(times)
+    line = {"metric": "64-map uneven batch: DFS nodes/s, one graph replay of the batched kernel",
+            "value": nodes / t, "unit": "nodes/s", "ms_per_step": 1e3 * t,
+            "higher_is_better": True, "scaling": "weak", "data": f"synthetic: uneven_instances(seed={seed})",
+            "config": {"workload": "64 uneven maps", "seed": seed,
+                       "block_threads": tuned["block_threads"], "node_budget": tuned["node_budget"],
+                       "depths": tuned["depths"]},
+            "plain_ms_per_step": 1e3 * plain_s, "batched_vs_plain": plain_s / t,
+            "gpu_launches": 2 * args.steps}
+    line.update(_gpu_common(args, clocks))
+    print(json.dumps(line), flush=True)
+
+
+def run_serving(args):
+    """Config 5: 8x8 chunk requests (MF_EXPANDED_N=36, 50,000 consecutive
+    cases from a seeded uniform start) arriving as a Poisson stream,
+    interleaved with whole maps up to 5x6, through one resident server.
+    Latency is submit -> result; every chunk is recounted alone afterwards
+    (which also gives the alone capacity) and every map checked against the
+    reference's counts."""
+    import map_folding_gb300 as mf
+    from map_folding_gb300.serving import Server, run_stream
+    from map_folding_gb300.workloads import serving_stream
+
+    reqs = serving_stream(seed=args.seed, requests=args.requests, rate_per_s=args.rate,
+                          chunk_cases=50_000)
+    golden = _golden_lunnon()
+    with Server() as srv:
+        # warm-up: the 8x8 expansion index and one small request of each kind
+        srv.wait(srv.submit_sym(8, 36, 0, 100))
+        srv.wait(srv.submit_lunnon((3, 4)))
+        with ClockSampler(0) as clocks:
+            out = run_stream(srv, reqs)
+    plan = mf.SymPlan(8, 36)
+    alone_s = 0.0
+    cases = 0
+    for r in out["results"]:
+        if r["kind"] == "chunk":
+            ans, st = plan.solve(r["max_cases"], r["start_case"], "batched")
+            assert ans == r["answer"], ("chunk differs from the chunk counted alone", r["rid"])
+            alone_s += st.kernel_s
+            r["alone_s"] = st.kernel_s
+            cases += r["max_cases"]
+        else:
+            key = "x".join(map(str, sorted(r["dims"])))  # p x q and q x p fold alike
+            assert r["answer"] == golden[key], (key, r["answer"])
+    plan.close()
+    line = {"metric": "8x8 chunk serving: chunk p99 latency (s) under a Poisson stream",
+            "value": out["chunk_p99_s"], "unit": "s", "higher_is_better": False,
+            "chunk_p50_s": out["chunk_p50_s"], "all_p50_s": out["all_p50_s"],
+            "all_p99_s": out["all_p99_s"], "cases_per_s": out["cases_per_s"],
+            "nodes_per_s": out["nodes_per_s"], "wall_s": out["wall_s"],
+            "alone_cases_per_s": cases / alone_s if alone_s else None,
+            "ms_per_step": 1e3 * out["wall_s"], "scaling": "weak",
+            "data": f"synthetic: serving_stream(seed={args.seed})",
+            "config": {"workload": "8x8 MF_EXPANDED_N=36 50,000-case chunks + maps <= 5x6",
+                       "requests": args.requests, "rate_per_s": args.rate,
+                       "chunks": sum(1 for r in out["results"] if r["kind"] == "chunk")},
+            "requests": [dict({k: r[k] for k in ("rid", "kind", "latency_s", "queue_s", "units")},
+                              arrival_s=q.arrival_s, alone_s=r.get("alone_s"))
+                         for r, q in zip(out["results"], reqs)],
+            "gpu_launches": None}
+    line.update(_gpu_common(args, clocks))
+    line["steps"] = 1
+    print(json.dumps(line), flush=True)
+
+
 def run_profile_case(case: str):
     """One launch of each kernel on a small case, for ncu (a few seconds of
     GPU work, inputs ~28 MB): `sym-partial` counts the 433,131 7x7 cases from
@@ -341,11 +506,22 @@ def main():
     ap.add_argument("--no-plain", dest="plain", action="store_false")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-case", default="", help="run one small case for ncu and exit")
+    # Supplementary workloads, one JSON line each; the default is the 7x7 count.
+    ap.add_argument("--workload", default="7x7", choices=["7x7", "lunnon", "uneven", "serving"])
+    ap.add_argument("--requests", type=int, default=12, help="serving: requests in the stream")
+    ap.add_argument("--rate", type=float, default=0.15, help="serving: Poisson arrivals per second")
+    ap.add_argument("--seed", type=int, default=5, help="serving: stream seed")
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args.profile_case)
     elif args.impl == "reference":
         run_reference(args)
+    elif args.workload == "lunnon":
+        run_lunnon(args)
+    elif args.workload == "uneven":
+        run_uneven(args)
+    elif args.workload == "serving":
+        run_serving(args)
     else:
         run_ours(args)
 

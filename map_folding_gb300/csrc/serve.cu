@@ -71,8 +71,16 @@ struct ServeCtl {
     unsigned int stop;             // host: leave once idle
     unsigned int error;
     long long idle_lanes;
-    unsigned long long pad[4];
+    unsigned int oldest_seq;       // host: oldest running request while others run, else 0
+    unsigned int pad0;
+    unsigned long long pad[3];
 };
+
+// Split items the oldest running request keeps in the ring while newer
+// requests share the GPU: lanes that free up (and find no unclaimed range)
+// take them before newer requests' subtrees, so the oldest request's heavy
+// subtrees spread over the lanes instead of finishing serially.
+constexpr long long kServeStock = 1024;
 
 struct ServeArgs {
     ServeCtl *ctl;
@@ -106,7 +114,7 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
     const unsigned lt_mask = (1u << lane) - 1u;
     bool busy = false, fresh = false;
     int lvl = 0, root = 0, last = 0, eval = 0;
-    uint32_t slot = 0, kind = 0, weight = 1;
+    uint32_t slot = 0, kind = 0, weight = 1, my_seq = 0;
     uint64_t mult = 1;
     SymRules srules = sym_rules(smem);
     LunnonRules lrules{A.tables, 0, 0};
@@ -131,6 +139,7 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
         slot = s;
         kind = I.kind;
         weight = I.weight;
+        my_seq = I.seq;
         last = I.last;
         S.base = I.base;
         if (kind == 0) srules = sym_rules(smem + (I.n - 6) * kSymTables);
@@ -162,7 +171,10 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
     };
 
     for (;;) {
-        // Refill idle lanes from the oldest published range.
+        // Refill idle lanes: units of the oldest published range first (a
+        // small request, or a large one admitted because lanes were idle),
+        // then split items, which come oldest request first while newer
+        // requests share the GPU.
         const unsigned need = __ballot_sync(kFull, !busy);
         if (need) {
             unsigned long long first = 0;
@@ -220,29 +232,29 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
                     eval = root;
                 }
             }
-            if (got < __popc(need) && ring_hint) {
-                // Split items for lanes the ranges could not feed.
-                const unsigned rest = __ballot_sync(kFull, !busy);
-                unsigned long long f2 = 0;
-                const int g2 = rest ? ring_claim(A.Q, &A.Q.hdr->spawn_head, __popc(rest), true, f2) : 0;
-                const int r2 = __popc(rest & lt_mask);
-                if (((rest >> lane) & 1u) && r2 < g2) {
-                    uint32_t w[24];
-                    ring_take(A.Q, f2 + r2, w);
+        }
+        if (ring_hint && __any_sync(kFull, !busy)) {
+            const unsigned rest = __ballot_sync(kFull, !busy);
+            unsigned long long f2 = 0;
+            const int g2 = ring_claim(A.Q, &A.Q.hdr->spawn_head, __popc(rest), true, f2);
+            const int r2 = __popc(rest & lt_mask);
+            if (((rest >> lane) & 1u) && r2 < g2) {
+                uint32_t w[24];
+                ring_take(A.Q, f2 + r2, w);
 #pragma unroll
-                    for (int k = 0; k < 17; ++k) L.set_word(k, w[k]);
-                    set_slot(w[17]);
-                    mult = uint64_t(w[22]) | (uint64_t(w[23]) << 32);
-                    root = int(w[20]);
-                    unit_nodes0 = nodes;
-                    lvl = root;
-                    S.set(root, uint64_t(w[18]) | (uint64_t(w[19]) << 32));
-                    eval = advance(L, S, lvl, root);
-                    fresh = false;
-                    busy = eval >= 0;
-                }
-                if (g2 < __popc(rest)) ring_hint = false;
+                for (int k = 0; k < 17; ++k) L.set_word(k, w[k]);
+                set_slot(w[17]);
+                mult = uint64_t(w[22]) | (uint64_t(w[23]) << 32);
+                root = int(w[20]);
+                unit_nodes0 = nodes;
+                lvl = root;
+                S.set(root, uint64_t(w[18]) | (uint64_t(w[19]) << 32));
+                eval = advance(L, S, lvl, root);
+                fresh = false;
+                busy = eval >= 0;
+                if (!busy) finish();
             }
+            if (g2 < __popc(rest)) ring_hint = false;
         }
         const bool bookkeeping = ++round >= A.period;
         if (!__any_sync(kFull, busy)) {
@@ -284,6 +296,7 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
         round = 0;
         const unsigned idle_mask = __ballot_sync(kFull, !busy);
         long long want = 0, queued = 0;
+        unsigned oldest = 0;
         if (lane == 0) {
             const int idle_now = __popc(idle_mask);
             if (idle_now != reported_idle) {
@@ -295,18 +308,24 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
             const bool ranges_left = vload(&A.ctl->head) < vload(&A.ctl->published);
             if (!ranges_left)
                 want = *reinterpret_cast<volatile long long *>(&A.ctl->idle_lanes) - queued;
+            if (queued < kServeStock)
+                oldest = *reinterpret_cast<volatile unsigned int *>(&A.ctl->oldest_seq);
         }
         want = __shfl_sync(kFull, want, 0);
+        oldest = __shfl_sync(kFull, oldest, 0);
         ring_hint = __shfl_sync(kFull, queued, 0) > 0;
-        if (want > 0) {
-            // Donate, as the batched kernels do, carrying slot and multiplier.
+        if (want > 0 || oldest != 0) {
+            // Donate, as the batched kernels do, carrying slot and multiplier:
+            // every lane when lanes are idle, else the oldest request's lanes
+            // to keep its stock of split items.
             int s = root;
             uint64_t m = 0;
             if (busy && !fresh) {
                 while (s < lvl && S.get(s) == 0) ++s;
                 m = S.get(s);
             }
-            const bool can = busy && !fresh && m != 0 && last - s >= kMinSplitHeight;
+            const bool can = busy && !fresh && m != 0 && last - s >= kMinSplitHeight &&
+                             (want > 0 || my_seq == oldest);
             const unsigned donors = __ballot_sync(kFull, can);
             if (donors) {
                 unsigned long long first = 0;
@@ -350,6 +369,7 @@ __global__ void serve_ring_init(unsigned long long *seq, unsigned long long capa
 }
 
 constexpr int kServeTPB = 128;
+constexpr double kBigHoldS = 0.05;
 constexpr int kServeLevels = 32;
 
 double mono() {
@@ -413,9 +433,17 @@ struct mf_server {
     std::vector<std::pair<uint64_t, uint64_t>> free_units;  // sorted [off, len)
     uint64_t next_id = 1;
     uint32_t next_seq = 1;
+    uint32_t oldest_written = 0;
     uint64_t published = 0;
     uint64_t table_cursor = 0;
     int running = 0;
+    int running_big = 0;        // running requests with more than small_units units
+    uint64_t small_units = 0;   // a quarter of the resident lanes
+    uint64_t lanes = 0;         // resident lanes of the server kernel
+    long long *h_idle = nullptr;  // pinned copy of the kernel's idle-lane count
+    double idle_checked = 0;
+    double big_admitted = 0;      // when the last large request was admitted
+    bool idle_seen = false;
     std::string failure;
     std::unordered_map<uint64_t, std::shared_ptr<SymPlan>> plans;
 };
@@ -500,20 +528,19 @@ bool admit(mf_server *s, const std::shared_ptr<Request> &r) {
         table_off = s->table_cursor;
         s->table_cursor += tb;
     }
-    if (n > s->stage_cap) {
-        if (s->h_stage) cudaFreeHost(s->h_stage);
-        s->stage_cap = pow2_at_least(n, 1024);
-        if (cudaMallocHost(&s->h_stage, s->stage_cap * sizeof(ServeUnit)) != cudaSuccess) {
-            s->h_stage = nullptr;
-            s->stage_cap = 0;
-            s->failure = "pinned staging allocation failed";
-            free_units(s, off, n);
-            return false;
+    // Units go through the fixed pinned staging buffer in pieces (freeing or
+    // growing pinned memory would wait for the resident kernel).
+    cudaStream_t c = s->cstream;
+    bool ok = true;
+    for (uint64_t k0 = 0; ok && k0 < n; k0 += s->stage_cap) {
+        const uint64_t m = std::min<uint64_t>(s->stage_cap, n - k0);
+        for (uint64_t k = 0; k < m; ++k) {
+            s->h_stage[k] = r->units[k0 + k];
+            s->h_stage[k].slot = uint32_t(slot);
         }
-    }
-    for (uint64_t k = 0; k < n; ++k) {
-        s->h_stage[k] = r->units[k];
-        s->h_stage[k].slot = uint32_t(slot);
+        ok = cudaMemcpyAsync(s->d_units + off + k0, s->h_stage, m * sizeof(ServeUnit),
+                             cudaMemcpyHostToDevice, c) == cudaSuccess &&
+             cudaStreamSynchronize(c) == cudaSuccess;
     }
     r->info.seq = s->next_seq++;
     r->info.table_off = uint32_t(table_off);
@@ -525,9 +552,6 @@ bool admit(mf_server *s, const std::shared_ptr<Request> &r) {
     const long long pend = (long long)n;
     const unsigned long long zero = 0;
     const uint64_t pub = s->published + 1;
-    cudaStream_t c = s->cstream;
-    bool ok = cudaMemcpyAsync(s->d_units + off, s->h_stage, n * sizeof(ServeUnit),
-                              cudaMemcpyHostToDevice, c) == cudaSuccess;
     if (r->info.kind == 1)
         ok = ok && cudaMemcpyAsync(s->d_tables + table_off, r->table.data(), r->table.size(),
                                    cudaMemcpyHostToDevice, c) == cudaSuccess;
@@ -551,7 +575,41 @@ bool admit(mf_server *s, const std::shared_ptr<Request> &r) {
     r->t_admit = mono();
     s->slot_req[size_t(slot)] = r;
     ++s->running;
+    if (r->unit_count > s->small_units) ++s->running_big;
     return true;
+}
+
+// Tell the kernel which request is the oldest while two or more share the
+// GPU (0 otherwise); its lanes then keep split items in stock.
+void publish_oldest(mf_server *s) {
+    uint32_t oldest = 0;
+    if (s->running >= 2)
+        for (const auto &r : s->slot_req)
+            if (r && (oldest == 0 || r->info.seq < oldest)) oldest = r->info.seq;
+    if (oldest == s->oldest_written) return;
+    if (cudaMemcpyAsync(&s->d_ctl->oldest_seq, &oldest, sizeof(oldest), cudaMemcpyHostToDevice,
+                        s->cstream) != cudaSuccess ||
+        cudaStreamSynchronize(s->cstream) != cudaSuccess) {
+        s->failure = "publishing the oldest request failed";
+        return;
+    }
+    s->oldest_written = oldest;
+}
+
+// True once at least 1/8 of the resident lanes are idle (sampled at most
+// every 0.5 ms): the running requests no longer fill the GPU.
+bool lanes_idle(mf_server *s) {
+    const double now = mono();
+    if (now - s->idle_checked < 5e-4) return s->idle_seen;
+    s->idle_checked = now;
+    if (cudaMemcpyAsync(s->h_idle, &s->d_ctl->idle_lanes, sizeof(long long),
+                        cudaMemcpyDeviceToHost, s->cstream) != cudaSuccess ||
+        cudaStreamSynchronize(s->cstream) != cudaSuccess) {
+        s->failure = "reading the idle-lane count failed";
+        return false;
+    }
+    s->idle_seen = *s->h_idle >= (long long)(s->lanes / 8);
+    return s->idle_seen;
 }
 
 void pump_loop(mf_server *s) {
@@ -573,12 +631,37 @@ void pump_loop(mf_server *s) {
             free_units(s, r->arena_off, r->units.size());
             r->units.clear();
             r->units.shrink_to_fit();
-            r.reset();
+            if (r->unit_count > s->small_units) --s->running_big;
             --s->running;
+            r.reset();
             s->cv.notify_all();
         }
-        // Admissions, first come first served.
-        while (!s->waiting.empty() && admit(s, s->waiting.front())) s->waiting.pop_front();
+        // Admissions. Large requests go first come first served, and the next
+        // one only once the running large requests leave lanes idle (work-
+        // conserving FIFO: a large request gets the whole GPU instead of
+        // sharing it and stretching everybody's latency). Small requests
+        // (whole small maps) are admitted at once.
+        bool big_blocked = false;
+        for (auto it = s->waiting.begin(); it != s->waiting.end();) {
+            const std::shared_ptr<Request> r = *it;
+            const bool big = r->unit_count > s->small_units;
+            // After a large admission the idle count needs a moment (its
+            // units being claimed) before it means anything again.
+            if (big && (big_blocked ||
+                        (s->running_big > 0 &&
+                         (mono() - s->big_admitted < kBigHoldS || !lanes_idle(s))))) {
+                big_blocked = true;
+                ++it;
+                continue;
+            }
+            if (!admit(s, r)) break;  // no slot or memory: keep the order
+            it = s->waiting.erase(it);
+            if (big) {
+                s->big_admitted = mono();
+                s->idle_checked = 0;  // sample afresh before the next one
+            }
+        }
+        publish_oldest(s);
         // Keep the kernel alive while work is resident.
         if (s->running > 0) {
             if (s->kernel_live && cudaStreamQuery(s->kstream) == cudaSuccess) s->kernel_live = false;
@@ -649,6 +732,9 @@ int make_server(const mf_server_config *cfg, mf_server **out) {
     serve_ring_init<<<64, 256>>>(s->Q.seq, s->Q.capacity);
     MF_TRY_CUDA(cudaGetLastError());
     MF_TRY_CUDA(cudaHostAlloc(&s->h_done, c.max_requests * sizeof(DoneRec), cudaHostAllocMapped));
+    s->stage_cap = std::min<uint64_t>(c.unit_capacity, 1ULL << 16);
+    MF_TRY_CUDA(cudaMallocHost(&s->h_idle, sizeof(long long)));
+    MF_TRY_CUDA(cudaMallocHost(&s->h_stage, s->stage_cap * sizeof(ServeUnit)));
     std::memset(static_cast<void *>(s->h_done), 0, c.max_requests * sizeof(DoneRec));
     MF_TRY_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->d_done), s->h_done, 0));
     s->smem = 3 * kSymTables + Carve<kServeTPB, 17, kServeLevels>::kThreadBytes;
@@ -662,6 +748,8 @@ int make_server(const mf_server_config *cfg, mf_server **out) {
         set_error("the server kernel does not fit on an SM");
         return MF_ERR_CUDA;
     }
+    s->lanes = uint64_t(s->sms) * uint64_t(s->blocks_per_sm) * kServeTPB;
+    s->small_units = s->lanes / 4;
     MF_TRY_CUDA(cudaDeviceSynchronize());
     s->slot_req.assign(c.max_requests, nullptr);
     s->free_units.push_back({0, c.unit_capacity});
@@ -917,6 +1005,7 @@ void mf_server_destroy(mf_server *s) {
     cudaFree(s->d_ring);
     cudaFreeHost(s->h_done);
     if (s->h_stage) cudaFreeHost(s->h_stage);
+    if (s->h_idle) cudaFreeHost(s->h_idle);
     cudaStreamDestroy(s->kstream);
     cudaStreamDestroy(s->cstream);
     delete s;
