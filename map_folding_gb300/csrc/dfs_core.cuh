@@ -70,37 +70,42 @@ __device__ __forceinline__ bool list_valid(const List<TPB> &L, int placed) {
 // positions landed on; AND the pages.  The pages' walks run as one flat loop
 // (a lane moves on to its next page inside the same loop), so a warp waits
 // for its longest lane's total walk, not for the sum of per-page maxima.
+// Both kinds of iteration -- starting a page and stepping along it -- end in
+// the same tail (mark the landed position, read its successor), so in a warp
+// whose lanes are at different kinds only the short heads diverge.  The pages
+// to walk for cell i are fixed by i alone and come packed from a per-cell
+// table: byte k = page << 6 | neighbour, `count` entries.
 struct SymRules {
-    const uint8_t *edge;  // 4 pages x 64, shared memory
-    const uint32_t *nb4;  // per cell: its 4 page neighbours, one byte each
+    const uint8_t *edge;     // 4 pages x 64, shared memory
+    const uint32_t *pages;   // per cell: its placed-neighbour pages, packed
+    const uint8_t *count;    // per cell: how many
     template <int TPB>
     __device__ __forceinline__ uint64_t gaps(const List<TPB> &L, int i,
                                              unsigned long long &nodes) const {
         ++nodes;
         uint64_t good = low_bits(i);
-        // Pages whose neighbour of i is placed: one word, four byte compares.
-        const uint32_t nb = nb4[i];
-        const uint32_t placed = __vcmpltu4(nb, 0x01010101u * uint32_t(i)) & 0x01010101u;
-        unsigned pend = (placed * 0x01020408u) >> 24;
+        uint32_t q = pages[i];
+        int left = count[i];
         const uint8_t *e = edge;
         uint64_t allowed = ~0ULL;
         int other = 0, j = 0;
         for (;;) {
+            int x;
             if (j == other) {  // current page finished (or none started)
                 good &= allowed;
-                if (!good || !pend) break;
-                const int p = __ffs(pend) - 1;
-                pend &= pend - 1;
-                e = edge + p * kSymCells;
-                other = (nb >> (8 * p)) & 0xff;
-                allowed = 1ULL << other;
-                j = L.get(other);
-                continue;
+                if (!good || !left) break;
+                --left;
+                other = q & 63;
+                e = edge + ((q >> 6) & 3) * kSymCells;
+                q >>= 8;
+                allowed = 0;
+                x = other;
+            } else {
+                const int partner = e[j];
+                x = partner < i ? partner : j;
             }
-            const int partner = e[j];
-            j = partner < i ? partner : j;
-            allowed |= 1ULL << j;
-            j = L.get(j);
+            allowed |= 1ULL << x;
+            j = L.get(x);
         }
         return good;
     }
@@ -327,23 +332,29 @@ __device__ __forceinline__ void run_units(const Rules &R, const List<TPB> &L, St
 
 // ---------------------------------------------------------- sym tables ---
 
-// Sym tables in shared memory: the 4 edge pages (256 B), then each cell's 4
-// page neighbours packed into one word (256 B).
-constexpr size_t kSymTables = 8 * kSymCells;
+// Sym tables in shared memory: the 4 edge pages (256 B), then per cell the
+// packed list of pages whose neighbour has a smaller number (256 B) and its
+// length (64 B).
+constexpr size_t kSymTables = 9 * kSymCells;
 
 template <int TPB>
 __device__ __forceinline__ void stage_sym_tables(uint8_t *smem, const uint8_t *__restrict__ edges) {
     for (int k = threadIdx.x; k < 64; k += TPB) {
         reinterpret_cast<uint32_t *>(smem)[k] = __ldg(reinterpret_cast<const uint32_t *>(edges) + k);
-        reinterpret_cast<uint32_t *>(smem + 4 * kSymCells)[k] =
-            uint32_t(__ldg(edges + k)) | (uint32_t(__ldg(edges + kSymCells + k)) << 8) |
-            (uint32_t(__ldg(edges + 2 * kSymCells + k)) << 16) |
-            (uint32_t(__ldg(edges + 3 * kSymCells + k)) << 24);
+        uint32_t q = 0;
+        int c = 0;
+        for (int p = 0; p < 4; ++p) {
+            const int nb = __ldg(edges + p * kSymCells + k);
+            if (nb < k) q |= uint32_t(nb | (p << 6)) << (8 * c++);
+        }
+        reinterpret_cast<uint32_t *>(smem + 4 * kSymCells)[k] = q;
+        smem[8 * kSymCells + k] = uint8_t(c);
     }
 }
 
 __device__ __forceinline__ SymRules sym_rules(const uint8_t *smem) {
-    return SymRules{smem, reinterpret_cast<const uint32_t *>(smem + 4 * kSymCells)};
+    return SymRules{smem, reinterpret_cast<const uint32_t *>(smem + 4 * kSymCells),
+                    smem + 8 * kSymCells};
 }
 
 // --------------------------------------------------------- split ring ----
