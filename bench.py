@@ -483,6 +483,16 @@ def run_profile_case(case: str):
         mf.count_cases_device(N, EXPANDED_N, 30, d_cyc.data_ptr(), len(cycles), d_counts.data_ptr())
         mf.count_cases_batched_device(N, EXPANDED_N, 30, d_cyc.data_ptr(), len(cycles),
                                       d_counts.data_ptr(), ws.data_ptr(), ws.numel())
+    elif case == "sym-steady":
+        # the bench's batched kernel on the first 20,000 7x7 cases, searched
+        # to completion (~2.6e10 nodes, under a second per launch)
+        plan = mf.SymPlan(N, EXPANDED_N)
+        cycles, _ = plan.cases(0, 20000)
+        d_cyc = torch.from_numpy(np.ascontiguousarray(cycles)).cuda()
+        d_counts = torch.zeros(len(cycles), dtype=torch.int64, device="cuda")
+        ws = torch.empty(mf.sym_workspace_bytes(), dtype=torch.uint8, device="cuda")
+        mf.count_cases_batched_device(N, EXPANDED_N, N * N, d_cyc.data_ptr(), len(cycles),
+                                      d_counts.data_ptr(), ws.data_ptr(), ws.numel())
     elif case == "lunnon":
         plan = mf.LunnonPlan((6, 6))
         for mode in ("plain", "batched"):
