@@ -461,6 +461,59 @@ def run_serving(args):
     print(json.dumps(line), flush=True)
 
 
+def run_chunk_plan(args):
+    """Equal-size chunks vs cost-weighted chunks (shallow estimate_work
+    lookahead): the whole 7x7 count in 40 chunks, and the 8x8 band of
+    1,000,000 cases at 50,000,000 (where the reference's slowest chunk
+    started) in 20 chunks; every chunk timed alone on the GPU, and each
+    plan's chunk sum checked against the other's."""
+    import numpy as np
+
+    import map_folding_gb300 as mf
+    from map_folding_gb300.chunks import plan_cost_chunks
+
+    def stats(times):
+        t = np.sort(np.asarray(times))
+        return {"chunks": len(t), "max_s": float(t[-1]), "p90_s": float(np.percentile(t, 90)),
+                "median_s": float(np.median(t)), "mean_s": float(t.mean()),
+                "max_over_mean": float(t[-1] / t.mean()), "sum_s": float(t.sum())}
+
+    out = {}
+    with ClockSampler(0) as clocks:
+        for name, n, e, start, count, k, depth in [("7x7_all", 7, 24, 0, 0, 40, args.cost_depth),
+                                                  ("8x8_d36_50M+1M", 8, 36, 50_000_000, 1_000_000,
+                                                   20, args.cost_depth)]:
+            plan = mf.SymPlan(n, e)
+            count = count or plan.total_cases
+            size = -(-count // k)
+            equal = [(s, min(size, start + count - s)) for s in range(start, start + count, size)]
+            t0 = time.perf_counter()
+            cost = plan_cost_chunks(n, e, k, depth, start, start + count, block=500)
+            plan_s = time.perf_counter() - t0
+            res = {}
+            for label, chunks in (("equal", equal), ("cost", cost)):
+                times, total = [], 0
+                for s, m in chunks:
+                    ans, st = plan.solve(m, s, "batched")
+                    times.append(st.kernel_s)
+                    total += ans
+                res[label] = dict(stats(times), answer=str(total),
+                                  sizes=[m for _, m in chunks])
+            plan.close()
+            assert res["equal"]["answer"] == res["cost"]["answer"], name
+            res["cost_depth"] = depth
+            res["plan_s"] = plan_s
+            out[name] = res
+    line = {"metric": "chunk time spread: max/mean of per-chunk GPU time, equal vs cost-weighted",
+            "value": out["8x8_d36_50M+1M"]["cost"]["max_over_mean"], "unit": "ratio",
+            "higher_is_better": False, "scaling": "weak", "data": "synthetic: exhaustive case ranges",
+            "config": {"workload": "7x7 all cases in 40 chunks; 8x8 d36 [50M, 51M) in 20 chunks",
+                       "cost_depth": args.cost_depth},
+            "results": out, "gpu_launches": None}
+    line.update(_gpu_common(args, clocks))
+    print(json.dumps(line), flush=True)
+
+
 def run_profile_case(case: str):
     """One launch of each kernel on a small case, for ncu (a few seconds of
     GPU work, inputs ~28 MB): `sym-partial` counts the 433,131 7x7 cases from
@@ -517,7 +570,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-case", default="", help="run one small case for ncu and exit")
     # Supplementary workloads, one JSON line each; the default is the 7x7 count.
-    ap.add_argument("--workload", default="7x7", choices=["7x7", "lunnon", "uneven", "serving"])
+    ap.add_argument("--workload", default="7x7",
+                    choices=["7x7", "lunnon", "uneven", "serving", "chunk-plan"])
+    ap.add_argument("--cost-depth", type=int, default=6, help="chunk-plan: lookahead depth")
     ap.add_argument("--requests", type=int, default=12, help="serving: requests in the stream")
     ap.add_argument("--rate", type=float, default=0.15, help="serving: Poisson arrivals per second")
     ap.add_argument("--seed", type=int, default=5, help="serving: stream seed")
@@ -532,6 +587,8 @@ def main():
         run_uneven(args)
     elif args.workload == "serving":
         run_serving(args)
+    elif args.workload == "chunk-plan":
+        run_chunk_plan(args)
     else:
         run_ours(args)
 

@@ -199,6 +199,38 @@ int32_t mf_sym_plan_solve(const mf_sym_plan *plan, uint64_t max_cases, uint64_t 
                           int32_t mode, const mf_batch_config *cfg, uint64_t *answer_lo_hi,
                           mf_run_stats *stats);
 
+/* MF_COST_DEPTH / MF_SORT_CASES of the materialized mode: score every case
+ * of the plan by its number of completions `cost_depth` cells further
+ * (counted on the GPU; min, max and the uint128 total come back) and, when
+ * order != 0, hold the cases in cost order (1: descending, 2: ascending,
+ * ties by multiplier) so that start_case / max_cases of mf_sym_plan_solve and
+ * mf_sym_cases index that order.  cost_depth <= 0 does nothing.
+ * Replaces: score_and_sort_cases, sym_fold.cpp:267-314 (estimate_work
+ * :235-250). */
+int32_t mf_sym_plan_score(mf_sym_plan *plan, int32_t cost_depth, int32_t order, int32_t mode,
+                          const mf_batch_config *cfg, uint64_t *min_score, uint64_t *max_score,
+                          uint64_t *total_score_lo_hi, mf_run_stats *stats);
+
+/* Cost estimate of the plan's cases [start_case, start_case + count) for
+ * cost-weighted chunking: each case scores estimate_work at cost_depth cells
+ * further, plus one for the case itself, and the scores are summed per
+ * block of `block` consecutive cases into block_costs[ceil(count / block)].
+ * Scoring runs on the GPU in bounded slices, so any range of an 8x8 plan
+ * fits.  No counterpart in the reference, whose chunks are equal case
+ * ranges (modal_sym.py:166-172); it uses estimate_work (sym_fold.cpp:235-250),
+ * the lookahead its notes propose for balancing (docs/8x8-method.md:128). */
+int32_t mf_sym_plan_block_costs(const mf_sym_plan *plan, uint64_t start_case, uint64_t count,
+                                int32_t cost_depth, uint64_t block, int32_t mode,
+                                const mf_batch_config *cfg, uint64_t *block_costs);
+
+/* The reference's cost order on the host: perm[k] = index of the k-th case
+ * after sorting by score (descending, or ascending when ascending != 0),
+ * ties by multiplier ascending, with the same (unstable) std::sort the
+ * reference uses, so equal keys land where they land there.
+ * Replaces: sym_fold.cpp:297-310. */
+int32_t mf_sym_sort_order(const uint64_t *scores, const uint64_t *mults, uint64_t count,
+                          int32_t ascending, uint64_t *perm);
+
 /* Allocation-free variant of mf_sym_count_cases_batched.  No counterpart in
  * the reference.  It is for callers that cannot allocate device memory at
  * all and therefore cannot pass a workspace: a process whose GPU memory is

@@ -276,6 +276,30 @@ class SymPlan:
         k = out.value
         return cyc[:k], mult[:k]
 
+    def score(self, cost_depth: int, order: str | None = None, mode: str | int = "batched",
+              cfg=None):
+        """MF_COST_DEPTH / MF_SORT_CASES (sym_fold.cpp:267-314): score every
+        case by its completions `cost_depth` cells further and, with order
+        "desc" or "asc", hold the cases in that order for later chunks.
+        Returns (min_score, max_score, total_score)."""
+        o = {None: 0, "desc": 1, "asc": 2}[order]
+        lo = ctypes.c_uint64()
+        hi = ctypes.c_uint64()
+        tot = (ctypes.c_uint64 * 2)()
+        check(_native.load().mf_sym_plan_score(self._h, cost_depth, o, _mode(mode), _cfg(cfg),
+                                               ctypes.byref(lo), ctypes.byref(hi), tot, None))
+        return lo.value, hi.value, _u128(tot)
+
+    def block_costs(self, start_case: int, count: int, cost_depth: int = 4, block: int = 1000,
+                    mode: str | int = "batched", cfg=None) -> np.ndarray:
+        """Estimated cost per block of `block` consecutive cases of
+        [start_case, start_case + count): each case's estimate_work score at
+        `cost_depth` cells further, plus one (mf_sym_plan_block_costs)."""
+        out = np.zeros(max((count + block - 1) // block, 1), np.uint64)
+        check(_native.load().mf_sym_plan_block_costs(self._h, start_case, count, cost_depth, block,
+                                                     _mode(mode), _cfg(cfg), out.ctypes.data))
+        return out[:(count + block - 1) // block]
+
     def solve(self, max_cases: int = 0, start_case: int = 0, mode: str | int = "batched",
               cfg=None):
         """(answer, RunStats) for the chunk, as `sym_fold` prints it."""
@@ -284,6 +308,17 @@ class SymPlan:
         check(_native.load().mf_sym_plan_solve(self._h, max_cases, start_case, _mode(mode),
                                                _cfg(cfg), ans, ctypes.byref(st)))
         return _u128(ans), st
+
+
+def sym_sort_order(scores, mults, ascending: bool = False) -> np.ndarray:
+    """The reference's cost order (sym_fold.cpp:297-310) on the host:
+    indices of the cases sorted by score, ties by multiplier."""
+    s = np.ascontiguousarray(scores, dtype=np.uint64)
+    m = np.ascontiguousarray(mults, dtype=np.uint64)
+    perm = np.zeros(max(len(s), 1), np.uint64)
+    check(_native.load().mf_sym_sort_order(s.ctypes.data, m.ctypes.data, len(s), int(ascending),
+                                           perm.ctypes.data))
+    return perm[:len(s)]
 
 
 def sym_fold(n: int, max_cases: int = 0, start_case: int = 0, expanded_n: int = 24,

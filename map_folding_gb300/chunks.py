@@ -11,6 +11,17 @@ modal_sym.py writes (sorted on write):
     python -m map_folding_gb300.chunks sweep --n 8 --expanded-n 36 \
         --chunk-size 50000 --chunk-count 4 --out results/8x8.jsonl
     python -m map_folding_gb300.chunks validate --out results/8x8.jsonl --chunk-size 50000
+
+Cost-weighted chunks (the balancing docs/8x8-method.md:128 proposes and the
+reference does not build): `plan_cost_chunks` scores every case with a
+shallow estimate_work lookahead on the GPU and cuts the case range into
+contiguous chunks of about equal estimated cost, so rows keep the
+(start_case, max_cases) form; `sweep(chunk_plan=...)` runs such a plan and
+`validate(..., chunk_size=0)` checks that the rows tile the case range.
+
+    python -m map_folding_gb300.chunks sweep --n 8 --expanded-n 36 \
+        --cost-depth 4 --chunk-count 4804 --out results/8x8-cost.jsonl
+    python -m map_folding_gb300.chunks validate --out results/8x8-cost.jsonl --chunk-size 0
 """
 from __future__ import annotations
 
@@ -36,7 +47,8 @@ def parse_result(stdout: str) -> str:
 
 
 def summarize_jsonl(path: Path, total_cases: int, chunk_size: int) -> dict:
-    """Coverage and sum of a sweep file (modal_sym.py:36-77)."""
+    """Coverage and sum of a sweep file (modal_sym.py:36-77).  chunk_size <=
+    0 means variable-size chunks: the rows must tile [0, total_cases)."""
     rows = []
     path = Path(path)
     if path.exists():
@@ -48,8 +60,6 @@ def summarize_jsonl(path: Path, total_cases: int, chunk_size: int) -> dict:
                 row = json.loads(text)
                 row["_line_no"] = line_no
                 rows.append(row)
-    expected_starts = list(range(0, total_cases, chunk_size))
-    expected_set = set(expected_starts)
     seen: dict[int, dict] = {}
     duplicate_starts = []
     for row in rows:
@@ -58,8 +68,25 @@ def summarize_jsonl(path: Path, total_cases: int, chunk_size: int) -> dict:
             duplicate_starts.append(start)
         else:
             seen[start] = row
-    missing = [s for s in expected_starts if s not in seen]
-    extra = sorted(s for s in seen if s not in expected_set)
+    if chunk_size > 0:
+        expected_starts = list(range(0, total_cases, chunk_size))
+        expected_set = set(expected_starts)
+        missing = [s for s in expected_starts if s not in seen]
+        extra = sorted(s for s in seen if s not in expected_set)
+    else:
+        # Variable chunks: walk the rows in start order; a gap is missing
+        # cases (reported by its first case), an overlap is extra.
+        missing, extra, pos = [], [], 0
+        for start in sorted(seen):
+            size = int(seen[start]["max_cases"])
+            if start > pos:
+                missing.append(pos)
+            elif start < pos:
+                extra.append(start)
+            pos = max(pos, start + size)
+        if pos < total_cases:
+            missing.append(pos)
+        expected_starts = sorted(seen) if not missing else sorted(seen) + missing
     unique_sum = sum(int(r["count"]) for r in seen.values())
     all_sum = sum(int(r["count"]) for r in rows)
     return {
@@ -75,7 +102,8 @@ def summarize_jsonl(path: Path, total_cases: int, chunk_size: int) -> dict:
         "extra_starts": extra[:20],
         "unique_sum": str(unique_sum),
         "all_rows_sum": str(all_sum),
-        "complete": len(seen) == len(expected_starts) and not duplicate_starts and not extra,
+        "complete": (not missing and not duplicate_starts and not extra and
+                     (chunk_size <= 0 or len(seen) == len(expected_starts))),
     }
 
 
@@ -143,17 +171,67 @@ class ChunkRunner:
                     wall_s, stderr)
 
 
+def plan_cost_chunks(n: int, expanded_n: int, chunk_count: int, cost_depth: int = 4,
+                     start_case: int = 0, total_cases: int = 0, block: int = 1000,
+                     mode: str = "batched") -> list[tuple[int, int]]:
+    """Contiguous chunks of about equal estimated cost over [start_case,
+    total_cases): block costs from the GPU (SymPlan.block_costs), then
+    boundaries where the cumulative cost crosses k / chunk_count of the total."""
+    from .api import SymPlan
+
+    plan = SymPlan(n, expanded_n)
+    try:
+        total_cases = total_cases or plan.total_cases
+        count = total_cases - start_case
+        costs = plan.block_costs(start_case, count, cost_depth, block, mode)
+    finally:
+        plan.close()
+    return partition_by_cost(costs, block, start_case, count, chunk_count)
+
+
+def partition_by_cost(costs, block: int, start_case: int, count: int,
+                      chunk_count: int) -> list[tuple[int, int]]:
+    """Cut [start_case, start_case + count) at block boundaries into at most
+    chunk_count contiguous, non-empty chunks of about equal summed cost."""
+    import numpy as np
+
+    if count <= 0 or chunk_count <= 0:
+        return []
+    csum = np.cumsum(np.asarray(costs, dtype=np.float64))
+    total = float(csum[-1]) if len(csum) else 0.0
+    cuts = [0]
+    for k in range(1, chunk_count):
+        b = int(np.searchsorted(csum, total * k / chunk_count, side="left")) + 1
+        b = min(b, len(csum))
+        if b > cuts[-1]:
+            cuts.append(b)
+    cases = [min(c * block, count) for c in cuts] + [count]
+    out = []
+    for a, b in zip(cases, cases[1:]):
+        if b > a:
+            out.append((start_case + a, b - a))
+    return out
+
+
 def sweep(n: int = 8, threads: int = 16, expanded_n: int = 36,
           total_cases: int = TOTAL_8X8_DEPTH36_CASES, chunk_size: int = 100000,
           start_case: int = 0, chunk_count: int = 0, out: str = "",
-          resume_existing: bool = False, mode: str = "batched", in_process: bool = True) -> dict:
-    """modal_sym.py:152-236 on the local GPU."""
-    if chunk_size <= 0:
-        raise ValueError("chunk_size must be positive")
-    starts = list(range(start_case, total_cases, chunk_size))
-    if chunk_count > 0:
-        starts = starts[:chunk_count]
-    inputs = [(s, min(chunk_size, total_cases - s)) for s in starts]
+          resume_existing: bool = False, mode: str = "batched", in_process: bool = True,
+          chunk_plan: list[tuple[int, int]] | None = None) -> dict:
+    """modal_sym.py:152-236 on the local GPU.  With chunk_plan, the given
+    (start_case, max_cases) chunks run instead of equal-size ones."""
+    if chunk_plan is not None:
+        inputs = [(int(s), int(m)) for s, m in chunk_plan]
+        if chunk_count > 0:
+            inputs = inputs[:chunk_count]
+        chunk_size = 0
+    else:
+        if chunk_size <= 0:
+            raise ValueError("chunk_size must be positive")
+        starts = list(range(start_case, total_cases, chunk_size))
+        if chunk_count > 0:
+            starts = starts[:chunk_count]
+        inputs = [(s, min(chunk_size, total_cases - s)) for s in starts]
     if not inputs:
         raise ValueError("No chunks selected")
     if not out:
@@ -233,6 +311,8 @@ def main(argv=None):
     s.add_argument("--resume-existing", action="store_true")
     s.add_argument("--mode", default="batched", choices=["plain", "batched"])
     s.add_argument("--cli", action="store_true", help="run each chunk through bin/sym_fold")
+    s.add_argument("--cost-depth", type=int, default=0,
+                   help="> 0: cost-weighted chunks (--chunk-count of them) scored this deep")
     v = sub.add_parser("validate")
     v.add_argument("--out", required=True)
     v.add_argument("--total-cases", type=int, default=TOTAL_8X8_DEPTH36_CASES)
@@ -240,8 +320,16 @@ def main(argv=None):
     v.add_argument("--expected", default="")
     a = ap.parse_args(argv)
     if a.cmd == "sweep":
+        chunk_plan = None
+        chunk_count = a.chunk_count
+        if a.cost_depth > 0:
+            if a.chunk_count <= 0:
+                ap.error("--cost-depth needs --chunk-count")
+            chunk_plan = plan_cost_chunks(a.n, a.expanded_n, a.chunk_count, a.cost_depth,
+                                          a.start_case, a.total_cases, mode=a.mode)
+            chunk_count = 0
         sweep(a.n, a.threads, a.expanded_n, a.total_cases, a.chunk_size, a.start_case,
-              a.chunk_count, a.out, a.resume_existing, a.mode, not a.cli)
+              chunk_count, a.out, a.resume_existing, a.mode, not a.cli, chunk_plan)
     else:
         validate(a.out, a.total_cases, a.chunk_size, a.expected)
 

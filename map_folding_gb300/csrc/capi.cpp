@@ -1041,6 +1041,125 @@ int32_t mf_sym_plan_solve(const mf_sym_plan *plan, uint64_t max_cases, uint64_t 
     return MF_OK;
 }
 
+int32_t mf_sym_plan_block_costs(const mf_sym_plan *plan, uint64_t start_case, uint64_t count,
+                                int32_t cost_depth, uint64_t block, int32_t mode,
+                                const mf_batch_config *cfg, uint64_t *block_costs) {
+    clear_error();
+    if (!plan || !block_costs || block == 0 || cost_depth < 0) {
+        set_error("plan, block_costs, block > 0 and cost_depth >= 0 are required");
+        return MF_ERR_ARG;
+    }
+    const SymPlan &p = plan->p;
+    if (start_case > p.total_cases || count > p.total_cases - start_case) {
+        set_error("case range [%llu, +%llu) is outside the plan's %llu cases",
+                  (unsigned long long)start_case, (unsigned long long)count,
+                  (unsigned long long)p.total_cases);
+        return MF_ERR_RANGE;
+    }
+    const uint64_t blocks = (count + block - 1) / block;
+    std::fill(block_costs, block_costs + blocks, 0ULL);
+    if (count == 0) return MF_OK;
+    int rc = ensure_device();
+    if (rc) return rc;
+    const int stop = std::min(p.n * p.n, p.start_i + cost_depth);
+    // Slices of whole blocks, about 2^21 cases each.
+    const uint64_t slice = std::max<uint64_t>(block, (uint64_t(1) << 21) / block * block);
+    std::vector<uint8_t> cycles(std::min(slice, count) * kSymCells);
+    std::vector<uint64_t> scores(std::min(slice, count) + 1);
+    for (uint64_t off = 0; off < count; off += slice) {
+        const uint64_t m = std::min(slice, count - off);
+        const uint64_t got = sym_select_cases(p, start_case + off, m, cycles.data(), nullptr, m);
+        if (got != m) {
+            set_error("case selection returned %llu of %llu cases", (unsigned long long)got,
+                      (unsigned long long)m);
+            return MF_ERR_RANGE;
+        }
+        mf_run_stats st{};
+        rc = count_cases_host(p.n, p.start_i, stop, cycles.data(), m, mode, cfg, scores.data(), &st,
+                              nullptr);
+        if (rc) return rc;
+        for (uint64_t k = 0; k < m; ++k) block_costs[(off + k) / block] += scores[k] + 1;
+    }
+    return MF_OK;
+}
+
+int32_t mf_sym_sort_order(const uint64_t *scores, const uint64_t *mults, uint64_t count,
+                          int32_t ascending, uint64_t *perm) {
+    clear_error();
+    if (count && (!scores || !mults || !perm)) {
+        set_error("scores, mults and perm are required");
+        return MF_ERR_ARG;
+    }
+    sym_sort_order(scores, mults, count, ascending != 0, perm);
+    return MF_OK;
+}
+
+int32_t mf_sym_plan_score(mf_sym_plan *plan, int32_t cost_depth, int32_t order, int32_t mode,
+                          const mf_batch_config *cfg, uint64_t *min_score, uint64_t *max_score,
+                          uint64_t *total_score_lo_hi, mf_run_stats *stats) {
+    clear_error();
+    if (!plan) {
+        set_error("plan is required");
+        return MF_ERR_ARG;
+    }
+    if (order < 0 || order > 2) {
+        set_error("order must be 0 (keep), 1 (descending) or 2 (ascending)");
+        return MF_ERR_ARG;
+    }
+    mf_run_stats local{};
+    mf_run_stats *st = stats ? stats : &local;
+    *st = mf_run_stats{};
+    if (min_score) *min_score = 0;
+    if (max_score) *max_score = 0;
+    if (total_score_lo_hi) total_score_lo_hi[0] = total_score_lo_hi[1] = 0;
+    SymPlan &p = plan->p;
+    // The cases in the order the plan holds them (the reference scores the
+    // list it holds: the expanded cases in emission order).
+    const uint64_t total = p.sorted_mult.empty() ? p.total_cases : p.sorted_mult.size();
+    if (cost_depth <= 0 || total == 0) return MF_OK;
+    int rc = ensure_device();
+    if (rc) return rc;
+    const double t0 = now_seconds();
+    std::vector<uint8_t> cycles(total * kSymCells);
+    std::vector<uint64_t> mults(total);
+    sym_select_cases(p, 0, total, cycles.data(), mults.data(), total);
+    // estimate_work counts the cycles that reach min(n2, start + depth)
+    // cells: the count kernels' partial-depth form.
+    const int stop = std::min(p.n * p.n, p.start_i + cost_depth);
+    std::vector<uint64_t> scores(total + 1);
+    rc = count_cases_host(p.n, p.start_i, stop, cycles.data(), total, mode, cfg, scores.data(), st,
+                          nullptr);
+    if (rc) return rc;
+    uint64_t lo = ~0ULL, hi = 0;
+    u128 sum = 0;
+    for (uint64_t k = 0; k < total; ++k) {
+        lo = std::min(lo, scores[k]);
+        hi = std::max(hi, scores[k]);
+        sum += scores[k];
+    }
+    if (min_score) *min_score = lo;
+    if (max_score) *max_score = hi;
+    if (total_score_lo_hi) {
+        total_score_lo_hi[0] = uint64_t(sum);
+        total_score_lo_hi[1] = uint64_t(sum >> 64);
+    }
+    if (order != 0) {
+        std::vector<uint64_t> perm(total);
+        sym_sort_order(scores.data(), mults.data(), total, order == 2, perm.data());
+        std::vector<uint8_t> sc(total * kSymCells);
+        std::vector<uint64_t> sm(total);
+        for (uint64_t k = 0; k < total; ++k) {
+            std::memcpy(&sc[k * kSymCells], &cycles[perm[k] * kSymCells], kSymCells);
+            sm[k] = mults[perm[k]];
+        }
+        p.sorted_cycles = std::move(sc);
+        p.sorted_mult = std::move(sm);
+    }
+    st->units = total;
+    st->total_s = now_seconds() - t0;
+    return MF_OK;
+}
+
 uint32_t mf_solve_cases(uint32_t n, uint32_t start_i, uint32_t stop_i, const uint8_t *case_buffer,
                         uint32_t case_count, uint32_t *output_words) {
     clear_error();

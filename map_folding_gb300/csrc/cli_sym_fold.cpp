@@ -136,6 +136,27 @@ int main(int argc, char **argv) {
             else
                 std::fprintf(stderr, "expanded_cases=%llu\n", (unsigned long long)total);
         }
+        // sym_fold.cpp:267-314 (materialized mode only): score by
+        // MF_COST_DEPTH, optionally reorder by MF_SORT_CASES.
+        const char *depth_text = std::getenv("MF_COST_DEPTH");
+        const int cost_depth = depth_text ? std::atoi(depth_text) : 0;
+        if (!stream && cost_depth > 0) {
+            const char *sort_text = std::getenv("MF_SORT_CASES");
+            int order = 0;
+            if (sort_text && *sort_text && std::strcmp(sort_text, "0") != 0)
+                order = std::strcmp(sort_text, "asc") == 0 ? 2 : 1;
+            uint64_t lo = 0, hi = 0, tot[2] = {0, 0};
+            const auto ts = Clock::now();
+            if (mf_sym_plan_score(plan, cost_depth, order, mode, nullptr, &lo, &hi, tot, nullptr) != MF_OK) {
+                std::fprintf(stderr, "error: %s\n", mf_last_error());
+                mf_sym_plan_destroy(plan);
+                return 2;
+            }
+            std::fprintf(stderr, "cost_depth=%d min_score=%llu max_score=%llu total_score=%s score_s=%g\n",
+                         cost_depth, (unsigned long long)lo, (unsigned long long)hi,
+                         decimal(tot[0], tot[1]).c_str(), since(ts));
+            if (order) std::fprintf(stderr, "sorted_cases=%s\n", order == 2 ? "asc" : "desc");
+        }
         if (std::getenv("MF_SETUP_ONLY") != nullptr) {
             // The reference prints the number of cases it holds: the centre
             // representatives in stream mode, the expanded cases otherwise.

@@ -79,7 +79,21 @@ struct SymPlan {
     std::vector<uint64_t> mid_mult;
     std::vector<uint64_t> mid_first;  // prefix sums: first case index of each
     uint64_t total_cases = 0;
+    // Once sorted by cost (MF_COST_DEPTH + MF_SORT_CASES, sym_fold.cpp:
+    // 267-314) the cases are held materialized in sorted order, and case
+    // indices refer to that order, as in the reference's materialized mode.
+    std::vector<uint8_t> sorted_cycles;
+    std::vector<uint64_t> sorted_mult;
 };
+
+// The reference's cost order (sym_fold.cpp:297-310): std::sort of the cases
+// by score, descending (ascending if `ascending`), ties by multiplier.
+// std::sort is not stable; given the same input order and comparator,
+// libstdc++'s introsort makes the same permutation whatever the element
+// type, so sorting (score, multiplier, index) triples reproduces the
+// reference's order.  perm[k] = emission index of the k-th sorted case.
+void sym_sort_order(const uint64_t *scores, const uint64_t *mults, uint64_t count, bool ascending,
+                    uint64_t *perm);
 
 // Builds reps/multipliers and (host side) the expansion index at mid level
 // `mid_i` (0 = none).  mid counts are filled by `count_below` when the

@@ -393,8 +393,36 @@ int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why) {
     return MF_OK;
 }
 
+void sym_sort_order(const uint64_t *scores, const uint64_t *mults, uint64_t count, bool ascending,
+                    uint64_t *perm) {
+    struct Scored {
+        uint64_t score;
+        uint64_t mult;
+        uint64_t index;
+    };
+    std::vector<Scored> v(count);
+    for (uint64_t k = 0; k < count; ++k) v[k] = Scored{scores[k], mults[k], k};
+    std::sort(v.begin(), v.end(), [&](const Scored &a, const Scored &b) {
+        if (a.score == b.score) return a.mult < b.mult;
+        return ascending ? a.score < b.score : a.score > b.score;
+    });
+    for (uint64_t k = 0; k < count; ++k) perm[k] = v[k].index;
+}
+
 uint64_t sym_select_cases(const SymPlan &plan, uint64_t start, uint64_t max_cases,
                           uint8_t *cycles, uint64_t *mults, uint64_t cap) {
+    if (!plan.sorted_mult.empty()) {  // cost-sorted order
+        const uint64_t total = plan.sorted_mult.size();
+        if (start >= total) return 0;
+        uint64_t end = total;
+        if (max_cases != 0 && max_cases < end - start) end = start + max_cases;
+        for (uint64_t k = start; k < end && k - start < cap; ++k) {
+            if (cycles) std::memcpy(cycles + (k - start) * kSymCells, &plan.sorted_cycles[k * kSymCells],
+                                    kSymCells);
+            if (mults) mults[k - start] = plan.sorted_mult[k];
+        }
+        return end - start;
+    }
     if (plan.mid_first.empty() || start >= plan.total_cases) return 0;
     uint64_t end = plan.total_cases;
     if (max_cases != 0 && max_cases < end - start) end = start + max_cases;

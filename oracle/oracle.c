@@ -709,6 +709,7 @@ int64_t orc_sym_expand(int32_t n, int32_t expanded_n, uint64_t start_case,
 typedef struct {
     const uint8_t *edges;
     int start_i, n2;
+    int stop;  /* count cycles reaching this many cells (n2: complete ones) */
     const uint8_t *cycles;
     const uint64_t *mults;
     int64_t count;
@@ -728,7 +729,9 @@ static void *sym_worker(void *arg) {
         if (k >= pool->count) break;
         uint8_t cy[SYM_CELLS];
         memcpy(cy, pool->cycles + k * SYM_CELLS, SYM_CELLS);
-        uint64_t c = orc_sym_count(cy, pool->start_i, pool->n2, pool->edges, &w);
+        uint64_t c = pool->stop >= pool->n2
+                         ? orc_sym_count(cy, pool->start_i, pool->n2, pool->edges, &w)
+                         : orc_sym_count_to(cy, pool->start_i, pool->stop, pool->edges, &w);
         if (pool->per_case) pool->per_case[k] = c;
         local += (u128)(pool->mults ? pool->mults[k] : 1) * (u128)c;
     }
@@ -740,7 +743,27 @@ static void *sym_worker(void *arg) {
     return NULL;
 }
 
+static void sym_run_pool(int32_t n, int32_t start_i, int32_t stop, const uint8_t *cycles,
+                         const uint64_t *mults, int64_t count, int32_t threads,
+                         uint64_t *per_case, uint64_t *sum_lo_hi, orc_work *work);
+
 void orc_sym_count_cases(int32_t n, int32_t start_i, const uint8_t *cycles,
+                         const uint64_t *mults, int64_t count, int32_t threads,
+                         uint64_t *per_case, uint64_t *sum_lo_hi, orc_work *work) {
+    sym_run_pool(n, start_i, n * n, cycles, mults, count, threads, per_case, sum_lo_hi, work);
+}
+
+/* sym_fold.cpp:235-250 (estimate_work), scored as score_and_sort_cases does
+ * at :274-283: each case's number of cycles reaching min(n2, start_i + depth)
+ * cells. */
+void orc_sym_estimate_cases(int32_t n, int32_t start_i, int32_t depth, const uint8_t *cycles,
+                            int64_t count, int32_t threads, uint64_t *scores) {
+    const int32_t n2 = n * n;
+    const int32_t stop = start_i + depth < n2 ? start_i + depth : n2;
+    sym_run_pool(n, start_i, stop, cycles, NULL, count, threads, scores, NULL, NULL);
+}
+
+static void sym_run_pool(int32_t n, int32_t start_i, int32_t stop, const uint8_t *cycles,
                          const uint64_t *mults, int64_t count, int32_t threads,
                          uint64_t *per_case, uint64_t *sum_lo_hi, orc_work *work) {
     uint8_t edges[4 * SYM_CELLS];
@@ -750,6 +773,7 @@ void orc_sym_count_cases(int32_t n, int32_t start_i, const uint8_t *cycles,
     pool.edges = edges;
     pool.start_i = start_i;
     pool.n2 = n * n;
+    pool.stop = stop;
     pool.cycles = cycles;
     pool.mults = mults;
     pool.count = count;

@@ -115,6 +115,12 @@ void orc_sym_count_cases(int32_t n, int32_t start_i, const uint8_t *cycles,
                          const uint64_t *mults, int64_t count, int32_t threads,
                          uint64_t *per_case, uint64_t *sum_lo_hi, orc_work *work);
 
+/* sym_fold.cpp:235-250 (estimate_work) as score_and_sort_cases applies it
+ * (:274-283): scores[k] = number of cycles of case k reaching
+ * min(n*n, start_i + depth) cells.  Threaded. */
+void orc_sym_estimate_cases(int32_t n, int32_t start_i, int32_t depth, const uint8_t *cycles,
+                            int64_t count, int32_t threads, uint64_t *scores);
+
 /* The whole sym_fold main (sym_fold.cpp:649-774) minus printing: returns the
  * 128-bit answer in out_lo_hi.  expanded_n <= 0 means the default 24.
  * Returns 0 on success, 1 on a bad argument (as the reference's rc 1). */

@@ -62,6 +62,8 @@ def lib():
         L.orc_sym_count_to.restype = _u64
         L.orc_sym_reps.argtypes = [_i32, _p, _p, _i64, ctypes.POINTER(_i64)]
         L.orc_sym_reps.restype = _i64
+        L.orc_sym_estimate_cases.argtypes = [_i32, _i32, _i32, _p, _i64, _i32, _p]
+        L.orc_sym_estimate_cases.restype = None
         L.orc_sym_expand.argtypes = [_i32, _i32, _u64, _u64, _p, _p, _i64]
         L.orc_sym_expand.restype = _i64
         L.orc_sym_count_cases.argtypes = [_i32, _i32, _p, _p, _i64, _i32, _p, _p,
@@ -174,6 +176,15 @@ def sym_expand(n: int, expanded_n: int, start_case: int = 0, max_cases: int = 0)
     lib().orc_sym_expand(n, expanded_n, start_case, max_cases, cyc.ctypes.data,
                          mult.ctypes.data, k)
     return cyc[:k], mult[:k]
+
+
+def sym_estimate_cases(n: int, start_i: int, depth: int, cycles, threads: int = 1) -> np.ndarray:
+    """Per-case estimate_work scores (sym_fold.cpp:235-250, :274-283)."""
+    cycles = np.ascontiguousarray(cycles, dtype=np.uint8)
+    scores = np.zeros(max(len(cycles), 1), np.uint64)
+    lib().orc_sym_estimate_cases(n, start_i, depth, cycles.ctypes.data, len(cycles), threads,
+                                 scores.ctypes.data)
+    return scores[:len(cycles)]
 
 
 def sym_count_cases(n: int, start_i: int, cycles, mults=None, threads: int = 1):

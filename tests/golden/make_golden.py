@@ -2,6 +2,7 @@
 solvers, built from source by `make -C oracle ref` into oracle/_ref/.
 
     python tests/golden/make_golden.py          # needs oracle/_ref/{mf,mf_fast,sym_fold}
+    python tests/golden/make_golden.py --cost   # refresh only the cost-order vectors
 
 Every value in the output was printed by an unmodified reference binary on
 this machine; published values quoted in the reference's documents are kept
@@ -27,6 +28,52 @@ def run(cmd, env=None):
     e.update(env or {})
     res = subprocess.run([str(c) for c in cmd], capture_output=True, text=True, env=e, check=True)
     return res.stdout.strip().splitlines()[0].strip()
+
+
+def run_with_stderr(cmd, env=None):
+    e = dict(os.environ)
+    e.update(env or {})
+    res = subprocess.run([str(c) for c in cmd], capture_output=True, text=True, env=e, check=True)
+    return res.stdout.strip().splitlines()[0].strip(), res.stderr
+
+
+def cost_jobs():
+    """Chunks of the materialized case list reordered by MF_COST_DEPTH /
+    MF_SORT_CASES (sym_fold.cpp:267-314).  Shallow depths give many equal
+    (score, multiplier) keys, so these pin the unstable sort's order too."""
+    return [
+        ("7x7_cost2_desc_300000+300", [REF / "sym_fold", 7, 8, 300, 300000],
+         {"MF_COST_DEPTH": "2", "MF_SORT_CASES": "1"}),
+        ("7x7_cost3_desc_200000+400", [REF / "sym_fold", 7, 8, 400, 200000],
+         {"MF_COST_DEPTH": "3", "MF_SORT_CASES": "desc"}),
+        ("7x7_cost1_desc_100000+300", [REF / "sym_fold", 7, 8, 300, 100000],
+         {"MF_COST_DEPTH": "1", "MF_SORT_CASES": "1"}),
+        ("7x7_cost4_asc_30000+300", [REF / "sym_fold", 7, 8, 300, 30000],
+         {"MF_COST_DEPTH": "4", "MF_SORT_CASES": "asc"}),
+        ("7x7_cost2_unsorted_first200", [REF / "sym_fold", 7, 8, 200, 0], {"MF_COST_DEPTH": "2"}),
+        ("6x6_cost3_desc_10+30", [REF / "sym_fold", 6, 8, 30, 10],
+         {"MF_COST_DEPTH": "3", "MF_SORT_CASES": "1"}),
+    ]
+
+
+def cost_result(cmd, env):
+    count, err = run_with_stderr(cmd, env)
+    line = next(ln for ln in err.splitlines() if ln.startswith("cost_depth="))
+    kv = dict(tok.split("=", 1) for tok in line.split())
+    return {"count": int(count), "min_score": int(kv["min_score"]),
+            "max_score": int(kv["max_score"]), "total_score": int(kv["total_score"]),
+            "env": env, "args": [str(c) for c in cmd[1:]]}
+
+
+def main_cost():
+    """Add (or refresh) only the cost-order vectors in reference_counts.json."""
+    path = HERE / "reference_counts.json"
+    out = json.loads(path.read_text())
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        futs = {k: ex.submit(cost_result, cmd, env) for k, cmd, env in cost_jobs()}
+        out["sym_cost"] = {k: f.result() for k, f in futs.items()}
+    path.write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
+    print(json.dumps(out["sym_cost"], indent=1, sort_keys=True))
 
 
 def lunnon_jobs():
@@ -113,6 +160,7 @@ def main():
         pf = {k: ex.submit(run, cmd, {"MF_COLLECT_ONLY": "1"}) for k, cmd in prefix_jobs()}
         sf = {k: ex.submit(run, cmd, env) for k, cmd, env in sym_jobs()}
         uf = {k: ex.submit(run, cmd, env) for k, cmd, env in setup_jobs()}
+        cf = {k: ex.submit(cost_result, cmd, env) for k, cmd, env in cost_jobs()}
         for k, f in lf.items():
             out["lunnon"][k] = int(f.result())
         for k, f in pf.items():
@@ -121,9 +169,13 @@ def main():
             out["sym"][k] = int(f.result())
         for k, f in uf.items():
             out["sym_setup"][k] = int(f.result())
+        out["sym_cost"] = {k: f.result() for k, f in cf.items()}
     (HERE / "reference_counts.json").write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
     print(json.dumps(out, indent=1, sort_keys=True))
 
 
 if __name__ == "__main__":
-    main()
+    if "--cost" in sys.argv:
+        main_cost()
+    else:
+        main()
