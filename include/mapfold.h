@@ -67,7 +67,8 @@ typedef struct {
     uint32_t hungry_factor;  /* split while queued items < factor/8 x threads */
     uint64_t queue_capacity; /* split-item ring cells (rounded up to a power of 2) */
     uint32_t wait_limit;     /* idle rounds before an idle warp leaves */
-    uint32_t stack_mode;     /* 0: DFS stack in shared memory when it fits, 1: local */
+    uint32_t stack_mode;     /* 0: DFS stack in shared memory when it fits, 1: local,
+                                2: sym counts on the 128-bit kernel whatever the board */
 } mf_batch_config;
 
 /* ======================================================================
@@ -148,9 +149,27 @@ typedef struct mf_sym_plan mf_sym_plan;
 
 /* Centre enumeration, D4 x stack-reversal dedup and the expansion index for
  * cases at `expanded_n` cells (0 = the reference default: 24 for n >= 7;
- * n = 6 always uses its 16-cell centre).  n must be 6..8.
+ * n = 6 always uses its 16-cell centre).  n must be 6..9.
  * Replaces: sym_fold.cpp:252-265, 316-408, 703-745. */
 int32_t mf_sym_plan_create(int32_t n, int32_t expanded_n, mf_sym_plan **out);
+
+/* Options of experiments/9x9/sym_fold9.cpp's setup (zero = default). */
+typedef struct {
+    int32_t expanded_n;   /* MF_EXPANDED_N (n >= 7): 0 = max(24, centre cells) */
+    int32_t center_n;     /* MF_CENTER_N: 0 = 3 odd, 4 even, 5 for 9x9; else 3..5, n's parity */
+    uint64_t seed_start;  /* MF_SEED_START: first centre representative kept */
+    uint64_t seed_count;  /* MF_SEED_COUNT: representatives kept (0 = the rest) */
+} mf_sym_plan_options;
+
+/* mf_sym_plan_create with sym_fold9's setup options; n may be 9.  Cases are
+ * expanded on the host to at most 64 cells (expanded_n <= 64), and counting
+ * past cell 63 runs on the 128-bit kernel.  A seed slice keeps centre
+ * representatives [seed_start, seed_start + seed_count) and numbers cases
+ * within the slice, as sym_fold9 does.
+ * Replaces: sym_fold9.cpp:969-981 (choose_center_size), :1037-1124 (setup;
+ * its MF_CENTER_STREAM_DEDUP and stored dedup give the same representatives
+ * in the same order). */
+int32_t mf_sym_plan_create_ex(int32_t n, const mf_sym_plan_options *opts, mf_sym_plan **out);
 void mf_sym_plan_destroy(mf_sym_plan *plan);
 /* Representatives before expansion and their orbit sizes. */
 int32_t mf_sym_plan_info(const mf_sym_plan *plan, int32_t *n, int32_t *start_i,

@@ -57,6 +57,15 @@ class BatchConfig(ctypes.Structure):
     ]
 
 
+class SymPlanOptions(ctypes.Structure):
+    _fields_ = [
+        ("expanded_n", ctypes.c_int32),
+        ("center_n", ctypes.c_int32),
+        ("seed_start", ctypes.c_uint64),
+        ("seed_count", ctypes.c_uint64),
+    ]
+
+
 class ServerConfig(ctypes.Structure):
     _fields_ = [
         ("unit_capacity", ctypes.c_uint64),
@@ -100,6 +109,7 @@ SIGNATURES = {
     "mf_lunnon_batch_count": ([_p, _i32, _p, _p, _p, _p], _i32),
     "mf_sym_edges": ([_i32, _p], _i32),
     "mf_sym_plan_create": ([_i32, _i32, ctypes.POINTER(_p)], _i32),
+    "mf_sym_plan_create_ex": ([_i32, _p, ctypes.POINTER(_p)], _i32),
     "mf_sym_plan_destroy": ([_p], None),
     "mf_sym_plan_info": ([_p, _p, _p, _p, _p, _p], _i32),
     "mf_sym_cases": ([_p, _u64, _u64, _p, _p, _u64, _pu64], _i32),

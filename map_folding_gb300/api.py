@@ -234,10 +234,12 @@ def sym_edges(n: int) -> np.ndarray:
 class SymPlan:
     """Centre representatives and the expansion index (sym_fold.cpp:703-745)."""
 
-    def __init__(self, n: int, expanded_n: int = 0):
+    def __init__(self, n: int, expanded_n: int = 0, center_n: int = 0, seed_start: int = 0,
+                 seed_count: int = 0):
         lib = _native.load()
         h = ctypes.c_void_p()
-        check(lib.mf_sym_plan_create(n, expanded_n, ctypes.byref(h)))
+        opts = _native.SymPlanOptions(expanded_n, center_n, seed_start, seed_count)
+        check(lib.mf_sym_plan_create_ex(n, ctypes.byref(opts), ctypes.byref(h)))
         self._h = h
         n_ = ctypes.c_int32()
         si = ctypes.c_int32()

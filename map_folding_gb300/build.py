@@ -25,9 +25,13 @@ BIN = PKG / "bin"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include")]
-LIB_SOURCES = ["host.cpp", "capi.cpp", "dfs_kernels.cu", "serve.cu"]
-CLI_SOURCES = {"gpu_folding": "cli_gpu_folding.cpp", "gpu_folding_v2": "cli_gpu_folding_v2.cpp",
-               "sym_fold": "cli_sym_fold.cpp"}
+LIB_SOURCES = ["host.cpp", "capi.cpp", "dfs_kernels.cu", "wide_kernels.cu", "serve.cu"]
+# name -> (source, extra compiler flags); sym_fold9 is sym_fold's source with
+# experiments/9x9/sym_fold9.cpp's options switched on.
+CLI_SOURCES = {"gpu_folding": ("cli_gpu_folding.cpp", []),
+               "gpu_folding_v2": ("cli_gpu_folding_v2.cpp", []),
+               "sym_fold": ("cli_sym_fold.cpp", []),
+               "sym_fold9": ("cli_sym_fold.cpp", ["-DMF_SYM_FOLD9"])}
 
 
 def nvcc() -> str:
@@ -64,11 +68,11 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append([cc, *COMMON, *ARCH, "-c", str(s), "-o", str(o)])
-    for name, src in CLI_SOURCES.items():
+    for name, (src, flags) in CLI_SOURCES.items():
         s = CSRC / src
-        o = OBJ / (s.stem + ".o")
+        o = OBJ / f"cli_{name}.o"
         if force or _stale(o, [s] + headers):
-            jobs.append([cc, *COMMON, "-c", str(s), "-o", str(o)])
+            jobs.append([cc, *COMMON, *flags, "-c", str(s), "-o", str(o)])
     workers = min(len(jobs), os.cpu_count() or 4) or 1
     with ThreadPoolExecutor(max_workers=workers) as ex:
         for cmd in jobs:
@@ -81,8 +85,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         tmp = LIB.with_suffix(".so.tmp")
         _run([cc, "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-lcudart"])
         os.replace(tmp, LIB)
-    for name, src in CLI_SOURCES.items():
-        o = OBJ / (Path(src).stem + ".o")
+    for name, (src, _) in CLI_SOURCES.items():
+        o = OBJ / f"cli_{name}.o"
         exe = BIN / name
         if force or _stale(exe, [o, LIB]):
             _run([cc, "-o", str(exe), str(o), f"-L{PKG}", "-lmapfold_gb300",

@@ -87,11 +87,14 @@ int ensure_device() {
 
 // Edge pages of each board size, uploaded once per device.
 std::mutex g_edges_mu;
-uint8_t *g_edges[16][9] = {};
+uint8_t *g_edges[16][10] = {};
+uint8_t *g_wide_edges[16][10] = {};
 
+// Boards over 64 cells get the 64-cell projection here (cells 0..63; the
+// host-side expansion and the index never go past 64 cells).
 const uint8_t *device_edges(int n) {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16 || n < 1 || n > 8) return nullptr;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16 || n < 1 || n > 9) return nullptr;
     std::lock_guard<std::mutex> lock(g_edges_mu);
     if (!g_edges[dev][n]) {
         uint8_t host[4 * kSymCells];
@@ -105,6 +108,25 @@ const uint8_t *device_edges(int n) {
         g_edges[dev][n] = d;
     }
     return g_edges[dev][n];
+}
+
+// Full edge pages (kWideCells per page) for the 128-bit kernel.
+const uint8_t *device_wide_edges(int n) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16 || n < 1 || n > 9) return nullptr;
+    std::lock_guard<std::mutex> lock(g_edges_mu);
+    if (!g_wide_edges[dev][n]) {
+        uint8_t host[4 * kWideCells];
+        sym_edges_stride(n, host, kWideCells);
+        uint8_t *d = nullptr;
+        if (cudaMalloc(&d, sizeof(host)) != cudaSuccess) return nullptr;
+        if (cudaMemcpy(d, host, sizeof(host), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaFree(d);
+            return nullptr;
+        }
+        g_wide_edges[dev][n] = d;
+    }
+    return g_wide_edges[dev][n];
 }
 
 struct Timer {
@@ -706,15 +728,23 @@ int32_t mf_sym_edges(int32_t n, uint8_t *out) {
 static int complete_index(SymPlan &p);
 
 int32_t mf_sym_plan_create(int32_t n, int32_t expanded_n, mf_sym_plan **out) {
+    mf_sym_plan_options o{};
+    o.expanded_n = expanded_n;
+    return mf_sym_plan_create_ex(n, &o, out);
+}
+
+int32_t mf_sym_plan_create_ex(int32_t n, const mf_sym_plan_options *opts, mf_sym_plan **out) {
     clear_error();
     if (!out) {
         set_error("out is NULL");
         return MF_ERR_ARG;
     }
     *out = nullptr;
+    mf_sym_plan_options o{};
+    if (opts) o = *opts;
     auto plan = std::make_unique<mf_sym_plan>();
     std::string why;
-    int rc = build_sym_plan(n, expanded_n, plan->p, why);
+    int rc = build_sym_plan(n, o.expanded_n, plan->p, why, o.center_n, o.seed_start, o.seed_count);
     if (rc) {
         set_error("%s", why.c_str());
         return rc;
@@ -756,7 +786,7 @@ int32_t mf_sym_plan_info(const mf_sym_plan *plan, int32_t *n, int32_t *start_i,
     if (n) *n = plan->p.n;
     if (start_i) *start_i = plan->p.start_i;
     if (center_cases) *center_cases = plan->p.center_cases;
-    if (reduced_cases) *reduced_cases = plan->p.rep_mult.size();
+    if (reduced_cases) *reduced_cases = plan->p.reduced_all;  // before any seed slice
     if (total_cases) *total_cases = plan->p.total_cases;
     return MF_OK;
 }
@@ -858,12 +888,18 @@ int count_cases_host(int n, int start_i, int stop_i, const uint8_t *h_cycles, ui
                      QueueHeader *hdr_out) {
     const size_t in_bytes = num * kSymCells;
     const BatchKnobs knobs = resolve_knobs(cfg);
+    // Searches past cell 63 run on the 128-bit kernel (batched only);
+    // stack_mode 2 selects it for any board.
+    const bool wide = stop_i > kSymCells || knobs.stack_mode == 2;
+    if (wide) mode = 1;
     auto *d_cycles = static_cast<uint8_t *>(scratch(kDevUnits, in_bytes, false));
     auto *d_counts = static_cast<uint64_t *>(scratch(kDevCounts, (num + 1) * 8, false));
-    void *d_work = mode == 1 ? scratch(kDevWork, workspace_bytes(knobs.queue_capacity), false) : nullptr;
+    const uint64_t ws_bytes = wide ? wide_workspace_bytes(knobs.queue_capacity)
+                                   : workspace_bytes(knobs.queue_capacity);
+    void *d_work = mode == 1 ? scratch(kDevWork, ws_bytes, false) : nullptr;
     auto *h_hdr = static_cast<uint8_t *>(scratch(kHostCounts, 256, true));
     if (!d_cycles || !d_counts || (mode == 1 && !d_work) || !h_hdr) return MF_ERR_CUDA;
-    const uint8_t *edges = device_edges(n);
+    const uint8_t *edges = wide ? device_wide_edges(n) : device_edges(n);
     if (!edges) {
         set_error("uploading the edge pages failed");
         return MF_ERR_CUDA;
@@ -875,7 +911,10 @@ int count_cases_host(int n, int start_i, int stop_i, const uint8_t *h_cycles, ui
     MF_TRY_CUDA(cudaMemsetAsync(d_counts + num, 0, 8, s));
     cudaEventRecord(th.b, s);
     cudaEventRecord(tk.a, s);
-    if (mode == 1)
+    if (wide)
+        MF_TRY_CUDA(launch_sym_wide(edges, start_i, stop_i, d_cycles, num, d_counts, d_counts + num,
+                                    d_work, knobs, s));
+    else if (mode == 1)
         MF_TRY_CUDA(launch_sym_batched(edges, start_i, stop_i, d_cycles, num, d_counts,
                                        d_counts + num, d_work, knobs, s));
     else

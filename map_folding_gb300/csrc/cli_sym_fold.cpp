@@ -7,6 +7,12 @@
 // MF_EXPANDED_N and MF_SETUP_ONLY.  The counting runs on the GPU; `threads`
 // is accepted and echoed.  MF_GPU_MODE=plain selects the one-thread-per-case
 // kernel instead of the batched work-stealing one.
+//
+// Built with -DMF_SYM_FOLD9 this is the drop-in for
+// experiments/9x9/sym_fold9.cpp instead: n up to 9, MF_CENTER_N (5x5 centre
+// by default on 9x9), MF_SEED_START / MF_SEED_COUNT and its stderr lines
+// (sym_fold9.cpp:963-1198); counting past cell 63 uses the 128-bit kernel.
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -54,6 +60,12 @@ void usage(const char *exe) {
 
 }  // namespace
 
+#ifdef MF_SYM_FOLD9
+constexpr long kMaxN = 9;
+#else
+constexpr long kMaxN = 8;
+#endif
+
 int main(int argc, char **argv) {
     if (argc < 2 || argc > 5) {
         usage(argv[0]);
@@ -64,8 +76,8 @@ int main(int argc, char **argv) {
         std::fprintf(stderr, "Invalid n: %s\n", argv[1]);
         return 2;
     }
-    if (n < 1 || n > 8) {
-        std::fprintf(stderr, "n must be between 1 and 8\n");
+    if (n < 1 || n > kMaxN) {
+        std::fprintf(stderr, "n must be between 1 and %ld\n", kMaxN);
         return 1;
     }
     unsigned hw = std::thread::hardware_concurrency();
@@ -114,25 +126,71 @@ int main(int argc, char **argv) {
         unsigned __int128 raw = a / (2 * n * n);
         std::fprintf(stderr, "raw_count=%s\n", decimal(uint64_t(raw), uint64_t(raw >> 64)).c_str());
     } else {
-        const int c2 = (n % 2 == 0) ? 16 : 9;
+        mf_sym_plan_options opts{};
+        int c = (n % 2 == 0) ? 4 : 3;
+#ifdef MF_SYM_FOLD9
+        // sym_fold9.cpp:969-981.
+        if (n >= 9) c = 5;
+        if (const char *text = std::getenv("MF_CENTER_N")) c = std::atoi(text);
+        if (c < 3 || c > n || c * c > 25 || (c % 2) != (n % 2)) {
+            std::fprintf(stderr,
+                         "MF_CENTER_N must be between 3 and %ld, have the same parity as n, and fit "
+                         "MAX_CENTER=25\n", n);
+            return 2;
+        }
+        opts.center_n = c;
+        unsigned long long seed_start = 0, seed_count = 0;
+        const char *seed_start_text = std::getenv("MF_SEED_START");
+        if (seed_start_text) {
+            if (!parse_size(seed_start_text, seed_start)) {
+                std::fprintf(stderr, "Invalid MF_SEED_START: %s\n", seed_start_text);
+                return 2;
+            }
+            if (const char *t = std::getenv("MF_SEED_COUNT")) {
+                if (!parse_size(t, seed_count)) {
+                    std::fprintf(stderr, "Invalid MF_SEED_COUNT: %s\n", t);
+                    return 2;
+                }
+            }
+            opts.seed_start = seed_start;
+            opts.seed_count = seed_count;
+        }
+        if (!std::getenv("MF_EXPANDED_N") && n >= 7) expanded_n = std::max(24, c * c);
+#endif
+        const int c2 = c * c;
         if (n >= 7 && (expanded_n < c2 || expanded_n > n * n)) {
             std::fprintf(stderr, "MF_EXPANDED_N must be between %d and %ld\n", c2, n * n);
             return 1;
         }
+        opts.expanded_n = n >= 7 ? expanded_n : 0;
         mf_sym_plan *plan = nullptr;
-        if (mf_sym_plan_create(int32_t(n), n >= 7 ? expanded_n : 0, &plan) != MF_OK) {
+        if (mf_sym_plan_create_ex(int32_t(n), &opts, &plan) != MF_OK) {
             std::fprintf(stderr, "error: %s\n", mf_last_error());
             return 2;
         }
         int32_t start_i = 0;
         uint64_t centers = 0, reduced = 0, total = 0;
         mf_sym_plan_info(plan, nullptr, &start_i, &centers, &reduced, &total);
+        unsigned long long seeds = reduced;  // representatives the cases come from
+#ifdef MF_SYM_FOLD9
+        std::fprintf(stderr, "center_size=%d center_cases=%llu%s\n", c, (unsigned long long)centers,
+                     std::getenv("MF_CENTER_STREAM_DEDUP") ? " center_stream_dedup=1" : "");
+        std::fprintf(stderr, "reduced_cases=%llu\n", (unsigned long long)reduced);
+        if (seed_start_text) {
+            const unsigned long long lo = std::min<unsigned long long>(seed_start, reduced);
+            const unsigned long long hi =
+                seed_count ? std::min<unsigned long long>(reduced, lo + seed_count) : reduced;
+            seeds = hi - lo;
+            std::fprintf(stderr, "seed_slice_start=%llu seed_slice_count=%llu\n", seed_start, seeds);
+        }
+#else
         std::fprintf(stderr, "center_cases=%llu\n", (unsigned long long)centers);
         std::fprintf(stderr, "reduced_cases=%llu\n", (unsigned long long)reduced);
+#endif
         if (n >= 7) {
             if (stream)
-                std::fprintf(stderr, "stream_seed_cases=%llu stream_from=%d stream_to=%d\n",
-                             (unsigned long long)reduced, c2, expanded_n);
+                std::fprintf(stderr, "stream_seed_cases=%llu stream_from=%d stream_to=%d\n", seeds, c2,
+                             expanded_n);
             else
                 std::fprintf(stderr, "expanded_cases=%llu\n", (unsigned long long)total);
         }
@@ -160,10 +218,22 @@ int main(int argc, char **argv) {
         if (std::getenv("MF_SETUP_ONLY") != nullptr) {
             // The reference prints the number of cases it holds: the centre
             // representatives in stream mode, the expanded cases otherwise.
+#ifdef MF_SYM_FOLD9
+            // sym_fold9.cpp:1145-1172: streaming past the centre prints the
+            // number of generated cases, otherwise the number of cases held.
+            const uint64_t held = (stream && start_i == c2) ? seeds : total;
+#else
             const uint64_t held = (n >= 7 && !stream) ? total : reduced;
+#endif
             std::printf("%llu\n", (unsigned long long)held);
+#ifdef MF_SYM_FOLD9
+            std::fprintf(stderr,
+                         "n=%ld threads=%ld center_n=%d max_cases=%llu start_case=%llu setup_only=1 "
+                         "total_s=%g\n", n, threads, c, max_cases, start_case, since(t0));
+#else
             std::fprintf(stderr, "n=%ld threads=%ld max_cases=%llu start_case=%llu setup_only=1 total_s=%g\n",
                          n, threads, max_cases, start_case, since(t0));
+#endif
             mf_sym_plan_destroy(plan);
             return 0;
         }

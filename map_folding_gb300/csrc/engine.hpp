@@ -57,8 +57,13 @@ int default_lunnon_depth(const LunnonTables &t);
 
 // --------------------------------------------------------------- sym -----
 constexpr int kSymCells = 64;
+// Boards over 64 cells (9x9, experiments/9x9/sym_fold9.cpp) search with
+// 128-bit masks over lists of up to kWideCells cells.
+constexpr int kWideCells = 96;
 
 void sym_edges(int n, uint8_t *out /* 4*64 */);
+// The same pages with `stride` cells each (cells >= stride left out).
+void sym_edges_stride(int n, uint8_t *out, int stride);
 uint64_t sym_good_host(const uint8_t *cycle, int i, const uint8_t *edges);
 
 struct SymPlan {
@@ -67,7 +72,10 @@ struct SymPlan {
     int seed_i = 0;       // c*c
     int start_i = 0;      // cells placed in every case (= expanded_n)
     uint64_t center_cases = 0;
-    std::vector<uint8_t> edges;      // 4*64
+    uint64_t seed_base = 0;           // first representative kept (seed slice)
+    uint64_t reduced_all = 0;         // representatives before the seed slice
+    std::vector<uint8_t> edges;      // 4*64 (boards over 64 cells: cells 0..63)
+    std::vector<uint8_t> wide_edges; // 4*kWideCells, boards over 64 cells only
     std::vector<uint8_t> reps;       // representatives, 64 bytes each
     std::vector<uint64_t> rep_mult;  // orbit sizes
     // Expansion index: the cases are the depth-start_i descendants of the
@@ -98,7 +106,10 @@ void sym_sort_order(const uint64_t *scores, const uint64_t *mults, uint64_t coun
 // Builds reps/multipliers and (host side) the expansion index at mid level
 // `mid_i` (0 = none).  mid counts are filled by `count_below` when the
 // index is used; see sym_plan_index().
-int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why);
+// center_n 0: default centre; a seed slice keeps representatives
+// [seed_start, seed_start + seed_count) (seed_count 0: the rest).
+int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why, int center_n = 0,
+                   uint64_t seed_start = 0, uint64_t seed_count = 0);
 
 // Enumerate depth-`stop` descendants of `cycle` (cells < from placed) in DFS
 // order, calling emit(cycle) for each; emit returns false to stop early.
@@ -151,6 +162,7 @@ struct QueueHeader {
 static_assert(sizeof(QueueHeader) == 64, "queue header layout");
 
 uint64_t workspace_bytes(uint64_t capacity);
+uint64_t wide_workspace_bytes(uint64_t capacity);
 
 // One Lunnon map as the batched kernel sees it.
 struct LunnonInstanceDev {
@@ -164,6 +176,14 @@ struct LunnonInstanceDev {
 cudaError_t launch_sym_plain(const uint8_t *d_edges, int start_i, int stop_i,
                              const uint8_t *d_cycles, uint64_t num, uint64_t *d_counts,
                              uint64_t *d_nodes, cudaStream_t stream);
+// The 128-bit batched search for boards over 64 cells (wide_kernels.cu):
+// d_wide_edges holds 4 pages of kWideCells, cases are 64-byte records with
+// start_i <= 64 cells placed, stop_i <= kWideCells.
+cudaError_t launch_sym_wide(const uint8_t *d_wide_edges, int start_i, int stop_i,
+                            const uint8_t *d_cycles, uint64_t num, uint64_t *d_counts,
+                            uint64_t *d_nodes, void *d_workspace, const BatchKnobs &knobs,
+                            cudaStream_t stream);
+
 cudaError_t launch_sym_batched(const uint8_t *d_edges, int start_i, int stop_i,
                                const uint8_t *d_cycles, uint64_t num, uint64_t *d_counts,
                                uint64_t *d_nodes, void *d_workspace, const BatchKnobs &knobs,

@@ -215,13 +215,16 @@ std::vector<int> spiral_numbers(int w, int h) {
 
 }  // namespace
 
-void sym_edges(int n, uint8_t *out) {
+void sym_edges_stride(int n, uint8_t *out, int stride) {
     const int cells = n * n;
-    std::memset(out, cells, 4 * kSymCells);
+    std::memset(out, cells, 4 * size_t(stride));
     auto num = spiral_numbers(n, n);
+    // Cells at or beyond `stride` get no entry (a 64-cell projection of a
+    // 9x9 board keeps cells 0..63 with partners up to 80, which every search
+    // below 64 cells treats as not yet placed).
     auto link = [&](int page, int u, int v) {
-        out[page * kSymCells + u] = uint8_t(v);
-        out[page * kSymCells + v] = uint8_t(u);
+        if (u < stride) out[page * stride + u] = uint8_t(v);
+        if (v < stride) out[page * stride + v] = uint8_t(u);
     };
     // sym_fold.cpp:147-173: x-edges go to page x%2, y-edges to page 2+y%2.
     for (int x = 0; x < n; ++x)
@@ -230,6 +233,8 @@ void sym_edges(int n, uint8_t *out) {
             if (y > 0) link(2 + y % 2, num[x * n + y], num[x * n + y - 1]);
         }
 }
+
+void sym_edges(int n, uint8_t *out) { sym_edges_stride(n, out, kSymCells); }
 
 // sym_fold.cpp:179-204.
 uint64_t sym_good_host(const uint8_t *cycle, int i, const uint8_t *edges) {
@@ -251,7 +256,8 @@ uint64_t sym_good_host(const uint8_t *cycle, int i, const uint8_t *edges) {
 
 namespace {
 
-using CenterKey = std::array<uint8_t, 16>;
+constexpr int kMaxCentre = 25;  // 5 x 5 centre (experiments/9x9/sym_fold9.cpp:33)
+using CenterKey = std::array<uint8_t, kMaxCentre>;
 
 struct CenterKeyHash {
     size_t operator()(const CenterKey &k) const {
@@ -270,7 +276,7 @@ CenterKey key_of(const uint8_t *cycle, int c2) {
 
 // The eight symmetries of the c x c centre as permutations of its own
 // spiral numbering (sym_fold.cpp:316-350).
-std::vector<std::array<uint8_t, 16>> centre_symmetries(int c) {
+std::vector<std::array<uint8_t, kMaxCentre>> centre_symmetries(int c) {
     auto num = spiral_numbers(c, c);
     std::vector<int> px(c * c), py(c * c);
     for (int x = 0; x < c; ++x)
@@ -279,9 +285,9 @@ std::vector<std::array<uint8_t, 16>> centre_symmetries(int c) {
             py[num[x * c + y]] = y;
         }
     const int e = c - 1;
-    std::vector<std::array<uint8_t, 16>> out;
+    std::vector<std::array<uint8_t, kMaxCentre>> out;
     for (int t = 0; t < 8; ++t) {
-        std::array<uint8_t, 16> perm;
+        std::array<uint8_t, kMaxCentre> perm;
         perm.fill(255);
         for (int v = 0; v < c * c; ++v) {
             int x = px[v], y = py[v];
@@ -304,18 +310,26 @@ std::vector<std::array<uint8_t, 16>> centre_symmetries(int c) {
 
 }  // namespace
 
-int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why) {
-    if (n < 6 || n > 8) {
-        why = "symmetry plan needs n in 6..8";
+int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why, int center_n,
+                   uint64_t seed_start, uint64_t seed_count) {
+    if (n < 6 || n > 9) {
+        why = "symmetry plan needs n in 6..9";
         return MF_ERR_ARG;
     }
     plan = SymPlan{};
     plan.n = n;
-    plan.c = (n % 2 == 0) ? 4 : 3;
+    // sym_fold.cpp:703 (c = 3 odd, 4 even); experiments/9x9/sym_fold9.cpp:
+    // 969-981 adds MF_CENTER_N and a 5x5 default for 9x9.
+    plan.c = center_n > 0 ? center_n : (n >= 9 ? 5 : ((n % 2 == 0) ? 4 : 3));
+    if (plan.c < 3 || plan.c > n || plan.c * plan.c > kMaxCentre || (plan.c % 2) != (n % 2)) {
+        why = "MF_CENTER_N must be between 3 and " + std::to_string(n) +
+              ", have the same parity as n, and fit a 5x5 centre";
+        return MF_ERR_ARG;
+    }
     plan.seed_i = plan.c * plan.c;
     const int n2 = n * n;
     if (n >= 7) {
-        if (expanded_n <= 0) expanded_n = 24;
+        if (expanded_n <= 0) expanded_n = std::max(24, plan.seed_i);
         if (expanded_n < plan.seed_i || expanded_n > n2) {
             why = "MF_EXPANDED_N must be between " + std::to_string(plan.seed_i) + " and " +
                   std::to_string(n2);
@@ -325,31 +339,37 @@ int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why) {
     } else {
         plan.start_i = plan.seed_i;
     }
+    if (plan.start_i > kSymCells) {
+        why = "cases are expanded on the host to at most " + std::to_string(kSymCells) + " cells";
+        return MF_ERR_ARG;
+    }
     plan.edges.resize(4 * kSymCells);
-    sym_edges(n, plan.edges.data());
+    sym_edges(n, plan.edges.data());  // boards over 64 cells: the 64-cell projection
+    if (n2 > kSymCells) {
+        plan.wide_edges.resize(4 * kWideCells);
+        sym_edges_stride(n, plan.wide_edges.data(), kWideCells);
+    }
     const uint8_t *edges = plan.edges.data();
 
-    // Centre cycles: every cycle of the c*c centre cells, sym_fold.cpp:703-707.
-    std::vector<uint8_t> centers;
+    // Centre cycles: every cycle of the c*c centre cells (sym_fold.cpp:703-707),
+    // deduplicated as they are generated (sym_fold9.cpp:601-627 gives the same
+    // representatives in the same order as deduplicating the stored list):
+    // orbit representatives under the square's symmetries and reversal of the
+    // stack, sym_fold.cpp:361-408; the multiplier is the orbit size.
     uint8_t cyc[kSymCells] = {0};
     cyc[0] = 1;
     cyc[1] = 2;
     cyc[2] = 0;
-    sym_expand(cyc, 3, plan.seed_i, edges, [&](const uint8_t *c) {
-        centers.insert(centers.end(), c, c + kSymCells);
-        return true;
-    });
-    plan.center_cases = centers.size() / kSymCells;
-
-    // Orbit representatives under the square's symmetries and reversal of
-    // the stack, sym_fold.cpp:361-408; the multiplier is the orbit size.
     const int c2 = plan.seed_i;
     auto perms = centre_symmetries(plan.c);
     std::unordered_set<CenterKey, CenterKeyHash> seen;
-    for (uint64_t k = 0; k < plan.center_cases; ++k) {
-        const uint8_t *cy = &centers[k * kSymCells];
-        if (seen.count(key_of(cy, c2))) continue;
-        std::set<CenterKey> orbit;
+    seen.reserve(c2 > 16 ? (size_t(1) << 22) : 4096);
+    plan.center_cases = 0;
+    sym_expand(cyc, 3, plan.seed_i, edges, [&](const uint8_t *cy) {
+        ++plan.center_cases;
+        if (seen.count(key_of(cy, c2))) return true;
+        std::array<CenterKey, 16> orbit;
+        int orbit_len = 0;
         for (const auto &perm : perms) {
             uint8_t img[kSymCells], rev[kSymCells];
             std::memcpy(img, cy, kSymCells);
@@ -360,12 +380,28 @@ int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why) {
                 rev[img[v]] = uint8_t(v);
                 v = img[v];
             } while (v != 0);
-            orbit.insert(key_of(img, c2));
-            orbit.insert(key_of(rev, c2));
+            orbit[orbit_len++] = key_of(img, c2);
+            orbit[orbit_len++] = key_of(rev, c2);
         }
+        std::sort(orbit.begin(), orbit.begin() + orbit_len);
+        const int distinct = int(std::unique(orbit.begin(), orbit.begin() + orbit_len) - orbit.begin());
         plan.reps.insert(plan.reps.end(), cy, cy + kSymCells);
-        plan.rep_mult.push_back(orbit.size());
-        seen.insert(orbit.begin(), orbit.end());
+        plan.rep_mult.push_back(uint64_t(distinct));
+        seen.insert(orbit.begin(), orbit.begin() + distinct);
+        return true;
+    });
+    plan.reduced_all = plan.rep_mult.size();
+    // sym_fold9.cpp:1071-1088: MF_SEED_START / MF_SEED_COUNT slice the
+    // representatives; case indices then run within the slice.
+    if (seed_start > 0 || seed_count > 0) {
+        const uint64_t reps = plan.rep_mult.size();
+        const uint64_t lo = std::min(seed_start, reps);
+        const uint64_t hi = seed_count ? std::min(reps, lo + seed_count) : reps;
+        plan.reps = std::vector<uint8_t>(plan.reps.begin() + long(lo * kSymCells),
+                                         plan.reps.begin() + long(hi * kSymCells));
+        plan.rep_mult = std::vector<uint64_t>(plan.rep_mult.begin() + long(lo),
+                                              plan.rep_mult.begin() + long(hi));
+        plan.seed_base = lo;
     }
 
     // Expansion index.  Up to depth 24 the prefixes are few enough (~0.4 M

@@ -3,6 +3,7 @@ solvers, built from source by `make -C oracle ref` into oracle/_ref/.
 
     python tests/golden/make_golden.py          # needs oracle/_ref/{mf,mf_fast,sym_fold}
     python tests/golden/make_golden.py --cost   # refresh only the cost-order vectors
+    python tests/golden/make_golden.py --sym9   # refresh only the sym_fold9 (9x9) vectors
 
 Every value in the output was printed by an unmodified reference binary on
 this machine; published values quoted in the reference's documents are kept
@@ -74,6 +75,54 @@ def main_cost():
         out["sym_cost"] = {k: f.result() for k, f in futs.items()}
     path.write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
     print(json.dumps(out["sym_cost"], indent=1, sort_keys=True))
+
+
+def sym9_jobs():
+    """experiments/9x9/sym_fold9.cpp (128-bit masks, 5x5 centre): 9x9 chunks
+    deep enough to finish in seconds, the 5x5 centre on 7x7, and the 128-bit
+    path on 8x8 (which must agree with sym_fold)."""
+    s9 = REF / "sym_fold9"
+    c5 = {"MF_CENTER_N": "5", "MF_CENTER_STREAM_DEDUP": "1", "MF_STREAM_CASES": "1"}
+    return [
+        ("9x9_c5_d42_first100", [s9, 9, 8, 100, 0], dict(c5, MF_EXPANDED_N="42")),
+        ("9x9_c5_d40_1000000+100", [s9, 9, 8, 100, 1000000], dict(c5, MF_EXPANDED_N="40")),
+        ("9x9_c5_d44_first300", [s9, 9, 8, 300, 0], dict(c5, MF_EXPANDED_N="44")),
+        ("9x9_c5_d48_5000+2000", [s9, 9, 8, 2000, 5000], dict(c5, MF_EXPANDED_N="48")),
+        ("7x7_c5_d30_first2000", [s9, 7, 8, 2000, 0], dict(c5, MF_EXPANDED_N="30")),
+        ("8x8_c4_d36_first200", [s9, 8, 8, 200, 0], {"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "36"}),
+        ("9x9_c5_seed1000x10_d44_20+300", [s9, 9, 8, 300, 20],
+         dict(c5, MF_EXPANDED_N="44", MF_SEED_START="1000", MF_SEED_COUNT="10")),
+    ]
+
+
+def sym9_setup():
+    """Centre statistics of the 9x9 5x5-centre setup (stderr key=value)."""
+    _, err = run_with_stderr([REF / "sym_fold9", 9, 1],
+                             {"MF_CENTER_N": "5", "MF_SETUP_ONLY": "1"})
+    out = {}
+    for line in err.splitlines():
+        for tok in line.split():
+            if "=" in tok:
+                k, v = tok.split("=", 1)
+                if k in ("center_size", "center_cases", "reduced_cases") and v.isdigit():
+                    out[k] = int(v)
+    return out
+
+
+def main_sym9():
+    """Add (or refresh) only the sym_fold9 vectors in reference_counts.json."""
+    path = HERE / "reference_counts.json"
+    out = json.loads(path.read_text())
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        futs = {k: ex.submit(run, cmd, env) for k, cmd, env in sym9_jobs()}
+        setup = ex.submit(sym9_setup)
+        out["sym9"] = {k: {"count": int(f.result()), "env": env,
+                           "args": [str(c) for c in cmd[1:]]}
+                       for (k, cmd, env), f in zip(sym9_jobs(), futs.values())}
+        out["sym9_setup"] = setup.result()
+    path.write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
+    print(json.dumps({"sym9": out["sym9"], "sym9_setup": out["sym9_setup"]}, indent=1,
+                     sort_keys=True))
 
 
 def lunnon_jobs():
@@ -149,7 +198,7 @@ PUBLISHED = {
 
 
 def main():
-    for b in ("mf", "mf_fast", "sym_fold"):
+    for b in ("mf", "mf_fast", "sym_fold", "sym_fold9"):
         if not (REF / b).exists():
             sys.exit(f"missing {REF / b}: run `make -C oracle ref` first")
     out = {"generated_by": "tests/golden/make_golden.py from oracle/_ref binaries",
@@ -161,6 +210,8 @@ def main():
         sf = {k: ex.submit(run, cmd, env) for k, cmd, env in sym_jobs()}
         uf = {k: ex.submit(run, cmd, env) for k, cmd, env in setup_jobs()}
         cf = {k: ex.submit(cost_result, cmd, env) for k, cmd, env in cost_jobs()}
+        nf = {k: ex.submit(run, cmd, env) for k, cmd, env in sym9_jobs()}
+        n9 = ex.submit(sym9_setup)
         for k, f in lf.items():
             out["lunnon"][k] = int(f.result())
         for k, f in pf.items():
@@ -170,6 +221,9 @@ def main():
         for k, f in uf.items():
             out["sym_setup"][k] = int(f.result())
         out["sym_cost"] = {k: f.result() for k, f in cf.items()}
+        out["sym9"] = {k: {"count": int(nf[k].result()), "env": env, "args": [str(c) for c in cmd[1:]]}
+                       for k, cmd, env in sym9_jobs()}
+        out["sym9_setup"] = n9.result()
     (HERE / "reference_counts.json").write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
     print(json.dumps(out, indent=1, sort_keys=True))
 
@@ -177,5 +231,7 @@ def main():
 if __name__ == "__main__":
     if "--cost" in sys.argv:
         main_cost()
+    elif "--sym9" in sys.argv:
+        main_sym9()
     else:
         main()
