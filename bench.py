@@ -514,6 +514,46 @@ def run_chunk_plan(args):
     print(json.dumps(line), flush=True)
 
 
+def run_nine(args):
+    """9x9 chunks of experiments/9x9/sym_fold9.cpp (5x5 centre, streamed
+    cases at MF_EXPANDED_N = 40..48) on the 128-bit kernel, each checked
+    against the reference's count; plan setup (centre enumeration, dedup,
+    expansion index) timed apart from the chunk's own count."""
+    import map_folding_gb300 as mf
+
+    golden = json.loads((ROOT / "tests" / "golden" / "reference_counts.json").read_text())["sym9"]
+    chunks = [("9x9_c5_d42_first100", 42, 100, 0), ("9x9_c5_d40_1000000+100", 40, 100, 1000000),
+              ("9x9_c5_d44_first300", 44, 300, 0), ("9x9_c5_d48_5000+2000", 48, 2000, 5000),
+              ("9x9_d42_first5000", 42, 5000, 0)]
+    plans, rows = {}, []
+    nodes = kernel = 0.0
+    with ClockSampler(0) as clocks:
+        for key, e, m, s in chunks:
+            if e not in plans:
+                t0 = time.perf_counter()
+                plans[e] = mf.SymPlan(9, e, center_n=5)
+                plans[e].setup_s = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            ans, st = plans[e].solve(m, s)
+            wall = time.perf_counter() - t0
+            if key in golden:
+                assert ans == golden[key]["count"], key
+            rows.append({"chunk": key, "cases": m, "kernel_s": st.kernel_s, "call_s": wall,
+                         "plan_setup_s": plans[e].setup_s, "nodes": int(st.nodes),
+                         "nodes_per_s": st.nodes / st.kernel_s, "answer": str(ans)})
+            nodes += st.nodes
+            kernel += st.kernel_s
+    for p in plans.values():
+        p.close()
+    line = {"metric": "9x9 sym chunks (5x5 centre): reference DFS nodes/s on the 128-bit kernel",
+            "value": nodes / kernel, "unit": "nodes/s", "higher_is_better": True,
+            "ms_per_step": 1e3 * kernel, "scaling": "weak", "data": "synthetic: exhaustive case ranges",
+            "config": {"workload": "9x9 MF_CENTER_N=5 streamed chunks, MF_EXPANDED_N 40..48"},
+            "chunks": rows, "gpu_launches": None}
+    line.update(_gpu_common(args, clocks))
+    print(json.dumps(line), flush=True)
+
+
 def run_profile_case(case: str):
     """One launch of each kernel on a small case, for ncu (a few seconds of
     GPU work, inputs ~28 MB): `sym-partial` counts the 433,131 7x7 cases from
@@ -571,7 +611,7 @@ def main():
     ap.add_argument("--profile-case", default="", help="run one small case for ncu and exit")
     # Supplementary workloads, one JSON line each; the default is the 7x7 count.
     ap.add_argument("--workload", default="7x7",
-                    choices=["7x7", "lunnon", "uneven", "serving", "chunk-plan"])
+                    choices=["7x7", "lunnon", "uneven", "serving", "chunk-plan", "9x9"])
     ap.add_argument("--cost-depth", type=int, default=6, help="chunk-plan: lookahead depth")
     ap.add_argument("--requests", type=int, default=12, help="serving: requests in the stream")
     ap.add_argument("--rate", type=float, default=0.15, help="serving: Poisson arrivals per second")
@@ -589,6 +629,8 @@ def main():
         run_serving(args)
     elif args.workload == "chunk-plan":
         run_chunk_plan(args)
+    elif args.workload == "9x9":
+        run_nine(args)
     else:
         run_ours(args)
 
