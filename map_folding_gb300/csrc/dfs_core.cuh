@@ -216,23 +216,41 @@ __device__ __forceinline__ int advance(const List<TPB> &L, Stk &S, int &lvl, int
     }
 }
 
-// Consume the evaluation g of level `eval`.  The last level is never
-// entered: its positions are counted and the item above it detached again.
-// Returns true when a fresh unit turns out to be finished by this round.
+// Consume the evaluation g of level `eval` and advance to the next node, with
+// g handed over in a register (a level that was just evaluated starts from g
+// instead of storing it to the stack and loading it straight back).  The
+// last level is never entered: its positions are counted and the item above
+// it detached again.  Returns the next level to evaluate, or -1 when the
+// unit's subtree is exhausted (or a fresh unit had nothing left to place).
 template <class Stk, int TPB>
-__device__ __forceinline__ bool apply(const List<TPB> &L, Stk &S, int &lvl, int eval, int root,
-                                      int last, bool fresh, uint64_t g,
-                                      unsigned long long &leaves) {
+__device__ __forceinline__ int apply_advance(const List<TPB> &L, Stk &S, int &lvl, int eval,
+                                             int root, int last, bool fresh, uint64_t g,
+                                             unsigned long long &leaves) {
+    uint64_t cur;
     if (eval == last) {
         leaves += __popcll(g);
-        if (fresh) return true;
+        if (fresh) return -1;  // a unit with nothing left to place
         L.put(S.pick(lvl), L.get(lvl));  // detach item lvl (= eval - 1)
-        return false;
+        cur = S.get(lvl);
+    } else {
+        lvl = eval;
+        cur = g;
     }
-    lvl = eval;
-    S.set(lvl, g);
-    (void)root;
-    return false;
+    for (;;) {
+        if (cur == 0) {
+            if (lvl == root) return -1;
+            --lvl;
+            L.put(S.pick(lvl), L.get(lvl));  // detach item lvl
+            cur = S.get(lvl);
+            continue;
+        }
+        const int j = __ffsll(static_cast<long long>(cur)) - 1;
+        S.set(lvl, cur & (cur - 1));
+        L.put(lvl, L.get(j));  // insert item lvl after j
+        L.put(j, lvl);
+        S.set_pick(lvl, j);
+        return lvl + 1;
+    }
 }
 
 template <int TPB, int WORDS>
@@ -319,13 +337,9 @@ __device__ __forceinline__ void run_units(const Rules &R, const List<TPB> &L, St
     while (__any_sync(kFull, busy)) {
         if (busy) {
             const uint64_t g = R.gaps(L, eval, nodes);
-            if (apply(L, S, lvl, eval, root, last, fresh, g, leaves)) {
-                busy = false;
-            } else {
-                fresh = false;
-                eval = advance(L, S, lvl, root);
-                busy = eval >= 0;
-            }
+            eval = apply_advance(L, S, lvl, eval, root, last, fresh, g, leaves);
+            fresh = false;
+            busy = eval >= 0;
         }
     }
 }

@@ -361,13 +361,9 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
             uint64_t g;
             if (kSym) g = srules.gaps(L, eval, nodes);
             else g = lrules.gaps(L, eval, nodes);
-            bool done = apply(L, S, lvl, eval, root, last, fresh, g, leaves);
-            if (!done) {
-                fresh = false;
-                eval = advance(L, S, lvl, root);
-                done = eval < 0;
-            }
-            if (done) {
+            eval = apply_advance(L, S, lvl, eval, root, last, fresh, g, leaves);
+            fresh = false;
+            if (eval < 0) {
                 flush();
                 busy = false;
             }

@@ -281,13 +281,9 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
         nap = 256;
         if (busy) {
             const uint64_t g = evaluate();
-            bool done = apply(L, S, lvl, eval, root, last, fresh, g, leaves);
-            if (!done) {
-                fresh = false;
-                eval = advance(L, S, lvl, root);
-                done = eval < 0;
-            }
-            if (done) {
+            eval = apply_advance(L, S, lvl, eval, root, last, fresh, g, leaves);
+            fresh = false;
+            if (eval < 0) {
                 finish();
                 busy = false;
             }
