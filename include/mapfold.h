@@ -137,7 +137,7 @@ int32_t mf_lunnon_batch_count(const mf_lunnon_plan *const *plans, int32_t num_pl
                               uint64_t *counts_out, mf_run_stats *stats);
 
 /* ======================================================================
- * sym_fold: symmetry-reduced square counting (n <= 8)
+ * sym_fold: symmetry-reduced square counting (n <= 8; plans up to 9x9)
  * ====================================================================== */
 
 /* The four edge pages of an n x n grid in centre-out spiral numbering:

@@ -48,7 +48,11 @@ struct Scratch {
     bool pinned = false;
 };
 
-std::mutex g_scratch_mu;
+// Every entry point that uses the scratch buffers holds this lock for its
+// whole run (recursive: one such entry point may call another), so calls
+// from several host threads are serialised instead of reallocating buffers
+// under each other's kernels.
+std::recursive_mutex g_scratch_mu;
 Scratch g_scratch[8];
 
 enum Slot { kDevUnits = 0, kDevCounts, kDevWork, kDevAux, kHostUnits, kHostCounts, kDevAux2, kSlots };
@@ -267,6 +271,7 @@ int32_t mf_lunnon_count_range(const mf_lunnon_plan *cplan, int32_t depth, uint64
                               uint64_t max_states, int32_t mode, const mf_batch_config *cfg,
                               uint64_t *count_out, uint64_t *states_out, mf_run_stats *stats) {
     clear_error();
+    std::lock_guard<std::recursive_mutex> scratch_lock(g_scratch_mu);
     auto *plan = const_cast<mf_lunnon_plan *>(cplan);
     if (!plan || !count_out) {
         set_error("plan and count_out are required");
@@ -339,6 +344,7 @@ static int32_t lunnon_batch_impl(const mf_lunnon_plan *const *plans, int32_t num
                                  const int32_t *depths, const uint64_t *firsts,
                                  const uint64_t *limits, const mf_batch_config *cfg,
                                  uint64_t *counts_out, mf_run_stats *stats) {
+    std::lock_guard<std::recursive_mutex> scratch_lock(g_scratch_mu);
     if (!plans || num_plans < 1 || !counts_out) {
         set_error("plans, num_plans >= 1 and counts_out are required");
         return MF_ERR_ARG;
@@ -886,6 +892,7 @@ namespace {
 int count_cases_host(int n, int start_i, int stop_i, const uint8_t *h_cycles, uint64_t num,
                      int mode, const mf_batch_config *cfg, uint64_t *h_counts, mf_run_stats *st,
                      QueueHeader *hdr_out) {
+    std::lock_guard<std::recursive_mutex> scratch_lock(g_scratch_mu);
     const size_t in_bytes = num * kSymCells;
     const BatchKnobs knobs = resolve_knobs(cfg);
     // Searches past cell 63 run on the 128-bit kernel (batched only);
@@ -1051,6 +1058,7 @@ int32_t mf_sym_plan_solve(const mf_sym_plan *plan, uint64_t max_cases, uint64_t 
         return MF_ERR_ARG;
     }
     answer_lo_hi[0] = answer_lo_hi[1] = 0;
+    std::lock_guard<std::recursive_mutex> scratch_lock(g_scratch_mu);
     mf_run_stats local{};
     mf_run_stats *st = stats ? stats : &local;
     *st = mf_run_stats{};
