@@ -37,6 +37,37 @@ METRIC = "7x7 sym_fold count: reference DFS nodes/s (recurse_count calls), batch
 UNIT = "nodes/s"
 
 
+# DRAM bytes per case of the batched kernel: read + write of the ncu capture
+# of the first 20,000 7x7 cases (2,106,880 + 1,431,552 bytes), per case.
+TRAFFIC_PER_CASE = (2_106_880 + 1_431_552) / 20_000
+
+
+def work_counts() -> dict:
+    """The whole 7x7 count's reference nodes and chain steps, counted by the
+    oracle (tests/golden/make_work_counts.py)."""
+    p = ROOT / "tests" / "golden" / "work_counts.json"
+    return json.loads(p.read_text()).get("7x7_d24_all", {}) if p.exists() else {}
+
+
+def issue_figures(nodes_per_step: int, t_step: float, clock_summary: dict) -> dict:
+    """Issue-slot view of the DFS kernel: chain steps (get_good walk
+    iterations) per second and per SMSP issue slot at the sampled SM clock."""
+    import torch
+
+    work = work_counts()
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = clock_summary.get("sm_mhz") or clock_summary.get("sm_max_mhz")
+    out = {"sms": sms, "sm_mhz": mhz, "nodes_match_oracle": None}
+    if work.get("steps"):
+        out["nodes_match_oracle"] = work.get("nodes") == nodes_per_step
+        steps_s = work["steps"] / t_step
+        out["chain_steps_per_s"] = steps_s
+        out["chain_steps_per_step"] = work["steps"]
+        if mhz:
+            out["chain_steps_per_issue_slot"] = steps_s / (sms * 4 * mhz * 1e6)
+    return out
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -257,10 +288,15 @@ def run_ours(args):
     algo_bytes = len(cycles) * (64 + 8)
     hbm_peak, peak_kind = peaks()
     achieved = algo_bytes / t_step / 1e9
+    clock_summary = clocks.summary()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": None,
+                "frac": achieved / hbm_peak,
+                # ncu DRAM read + write of the first-20,000-case launch (3.54 MB,
+                # profiles/sym_batched_7x7_first20k.md) scaled by the case count
+                "traffic": TRAFFIC_PER_CASE * len(cycles), "traffic_unit": "bytes per launch",
                 "peak_source": peak_kind,
-                "note": "integer-issue/latency-bound DFS; HBM carries only the case loads"}
+                "note": "integer-issue/latency-bound DFS; HBM carries only the case loads",
+                "issue": issue_figures(nodes_per_step, t_step, clock_summary)}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -286,7 +322,7 @@ def run_ours(args):
             "gpu_launches": 2 * args.steps,
             "roofline": roofline,
             "cpu_baseline": cpu,
-            "clocks": clocks.summary(),
+            "clocks": clock_summary,
             "plain_ms_per_step": None if plain_s is None else 1e3 * plain_s,
             "batched_vs_plain": None if plain_s is None else plain_s / t_step,
             "splits_per_step": int(e2e_st.splits) if e2e_st else None,
@@ -346,7 +382,26 @@ def run_lunnon(args):
             tot_nodes += nodes
             tot_b += b
             tot_p += sp.kernel_s
+    # CPU baseline: the oracle's restatement of mf_fast.cpp's threaded resume
+    # (mf_fast <n> <depth> $(nproc)) on 6x6 at depth 18, all host threads.
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle
+
+        threads = os.cpu_count() or 1
+        a, b, _ = oracle.lunnon_collect((6, 6), 18)
+        count = 512
+        while True:  # grow a prefix of the states until one run takes ~10 s
+            t0 = time.perf_counter()
+            _, _, w = oracle.lunnon_resume_many((6, 6), 19, a[:count], b[:count], threads)
+            el = time.perf_counter() - t0
+            if el >= 5.0 or count >= len(a):
+                break
+            count = min(len(a), int(count * max(2.0, 10.0 / max(el, 1e-3))))
+        cpu = {"value": w.nodes / el, "unit": "nodes/s", "cores": threads, "kind": "port",
+               "sample": f"first {count} of {len(a)} 6x6 depth-18 prefix states ({el:.2f} s)"}
     line = {"metric": "Lunnon DFS nodes/s over configs 1-2 (5x5@15, 6x6@18, 20 rectangles, strips 8..20)",
+            "cpu_baseline": cpu,
             "value": tot_nodes / tot_b, "unit": "nodes/s", "ms_per_step": 1e3 * tot_b,
             "higher_is_better": True, "scaling": "weak", "data": "synthetic: exhaustive map counts",
             "config": {"workload": "lunnon maps", "maps": len(rows)},

@@ -1,0 +1,49 @@
+"""Generate tests/golden/work_counts.json: the algorithmic work of the bench
+workload, counted by the CPU oracle (oracle/oracle.c).
+
+    python tests/golden/make_work_counts.py      # ~35 min on 8 cores
+
+For the whole 7x7 count (all 433,131 cases at MF_EXPANDED_N=24) it records
+the reference nodes (recurse_count calls, sym_fold.cpp:219) and the chain
+steps (iterations of get_good's cycle walk, sym_fold.cpp:189-196).  These are
+the per-step work figures bench.py quotes throughput in; the GPU kernel's own
+node counter must equal `nodes` (bench.py checks the count and reports both).
+Unlike reference_counts.json these numbers come from the oracle, not from a
+reference binary; the oracle is pinned to the reference by the tests.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import time
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent.parent))
+
+
+def main():
+    from oracle import oracle
+
+    threads = os.cpu_count() or 1
+    cyc, mult = oracle.sym_expand(7, 24, 0, 0)
+    t0 = time.time()
+    total, _, w = oracle.sym_count_cases(7, 24, cyc, mult, threads)
+    out = {
+        "generated_by": "tests/golden/make_work_counts.py (oracle/oracle.c work counters)",
+        "7x7_d24_all": {
+            "cases": int(len(cyc)),
+            "answer": int(total) * 49,
+            "nodes": int(w.nodes),
+            "steps": int(w.steps),
+            "cpu_s": round(time.time() - t0, 1),
+            "cpu_threads": threads,
+        },
+    }
+    (HERE / "work_counts.json").write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
+    print(json.dumps(out, indent=1, sort_keys=True))
+
+
+if __name__ == "__main__":
+    main()
