@@ -112,21 +112,25 @@ __device__ __forceinline__ SymRulesW wide_rules(const uint8_t *smem) {
                      smem + kWidePages + 8 * kWideCells};
 }
 
-// 128-bit mask stack: level k's low word at lo[k*TPB], its high word LEVELS
-// rows further; the chosen positions as interleaved bytes.
+// 128-bit mask stack.  The mask of level lvl holds positions below lvl, so
+// its high word can be non-zero only for lvl > 64: low words get one row per
+// level (level k at lo[k*TPB]), high words rows only for levels 65 ..
+// 64 + kWideHiRows (after the low rows), and the other levels read zero.
+// The chosen positions are interleaved bytes.
+constexpr int kWideHiRows = 16;  // levels 65..80: enough below 82 cells
+
 template <int TPB, int LEVELS>
 struct StackW {
     uint64_t *lo;
     List<TPB> chosen;
     int base;
     __device__ __forceinline__ Mask128 get(int lvl) const {
-        const int k = (lvl - base) * TPB;
-        return Mask128{lo[k], lo[k + LEVELS * TPB]};
+        const uint64_t hi = lvl > 64 ? lo[(LEVELS + lvl - 65) * TPB] : 0ULL;
+        return Mask128{lo[(lvl - base) * TPB], hi};
     }
     __device__ __forceinline__ void set(int lvl, const Mask128 &v) const {
-        const int k = (lvl - base) * TPB;
-        lo[k] = v.lo;
-        lo[k + LEVELS * TPB] = v.hi;
+        lo[(lvl - base) * TPB] = v.lo;
+        if (lvl > 64) lo[(LEVELS + lvl - 65) * TPB] = v.hi;
     }
     __device__ __forceinline__ int pick(int lvl) const { return chosen.get(lvl - base); }
     __device__ __forceinline__ void set_pick(int lvl, int j) const { chosen.put(lvl - base, j); }
@@ -135,7 +139,7 @@ struct StackW {
 template <int TPB, int LEVELS>
 struct CarveW {
     static constexpr size_t kList = size_t(kWideWords) * 4 * TPB;
-    static constexpr size_t kMask = size_t(2 * LEVELS) * 8 * TPB;
+    static constexpr size_t kMask = size_t(LEVELS + kWideHiRows) * 8 * TPB;
     static constexpr size_t kPick = size_t((LEVELS + 3) / 4) * 4 * TPB;
     static constexpr size_t kBytes = kWideTables + kList + kMask + kPick;
 };
@@ -499,7 +503,10 @@ cudaError_t launch_sym_wide(const uint8_t *d_wide_edges, int start_i, int stop_i
     e = cudaMemsetAsync(d_counts, 0, num * sizeof(uint64_t), stream);
     if (e != cudaSuccess) return e;
     const int levels = stop_i - 1 - start_i;
-    if (start_i > kSymCells || stop_i > kWideCells) return cudaErrorInvalidValue;
+    // Stored levels run up to stop_i - 2; their high words need rows up to
+    // stop_i - 2 - 65 < kWideHiRows.
+    if (start_i > kSymCells || stop_i > 66 + kWideHiRows || stop_i > kWideCells)
+        return cudaErrorInvalidValue;
     if (levels <= 40)
         return launch_wide_levels<40>(d_wide_edges, start_i, stop_i - 1, d_cycles, num, d_counts,
                                       d_nodes, Q, slots, knobs, stream);
