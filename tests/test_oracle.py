@@ -101,3 +101,14 @@ def test_sym_node_counts_are_consistent(orc):
         w2 += w1.nodes
     # count_to also counts the calls at the stop level (one per completion)
     assert w2 == w.nodes + t1
+
+
+def test_work_counts_fixture_is_consistent(golden):
+    """The oracle's whole-7x7 work totals (tests/golden/work_counts.json)
+    belong to the published 7x7 answer."""
+    import json
+    from pathlib import Path
+
+    w = json.loads((Path(__file__).parent / "golden" / "work_counts.json").read_text())["7x7_d24_all"]
+    assert w["answer"] == golden["published"]["squares"]["7"]
+    assert w["cases"] == 433131 and w["steps"] > w["nodes"] > 0
