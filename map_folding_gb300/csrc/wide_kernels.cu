@@ -144,7 +144,7 @@ struct CarveW {
     static constexpr size_t kBytes = kWideTables + kList + kMask + kPick;
 };
 
-// advance / apply of dfs_core.cuh with 128-bit masks.
+// advance of dfs_core.cuh with 128-bit masks (a taken split item starts here).
 template <int TPB, int LEVELS>
 __device__ __forceinline__ int advance_w(const List<TPB> &L, const StackW<TPB, LEVELS> &S, int &lvl,
                                          int root) {
@@ -165,19 +165,38 @@ __device__ __forceinline__ int advance_w(const List<TPB> &L, const StackW<TPB, L
     }
 }
 
+// apply_advance of dfs_core.cuh with 128-bit masks: consume level eval's
+// mask g (handed over in registers) and move to the next node; -1 when the
+// unit's subtree is exhausted.
 template <int TPB, int LEVELS>
-__device__ __forceinline__ bool apply_w(const List<TPB> &L, const StackW<TPB, LEVELS> &S, int &lvl,
-                                        int eval, int last, bool fresh, const Mask128 &g,
-                                        unsigned long long &leaves) {
+__device__ __forceinline__ int apply_advance_w(const List<TPB> &L, const StackW<TPB, LEVELS> &S,
+                                               int &lvl, int eval, int root, int last, bool fresh,
+                                               const Mask128 &g, unsigned long long &leaves) {
+    Mask128 cur;
     if (eval == last) {
         leaves += w_popc(g);
-        if (fresh) return true;
-        L.put(S.pick(lvl), L.get(lvl));
-        return false;
+        if (fresh) return -1;
+        L.put(S.pick(lvl), L.get(lvl));  // detach item lvl (= eval - 1)
+        cur = S.get(lvl);
+    } else {
+        lvl = eval;
+        cur = g;
     }
-    lvl = eval;
-    S.set(lvl, g);
-    return false;
+    for (;;) {
+        if (w_zero(cur)) {
+            if (lvl == root) return -1;
+            --lvl;
+            L.put(S.pick(lvl), L.get(lvl));  // detach item lvl
+            cur = S.get(lvl);
+            continue;
+        }
+        const int j = w_low(cur);
+        S.set(lvl, w_drop_low(cur));
+        L.put(lvl, L.get(j));  // insert item lvl after j
+        L.put(j, lvl);
+        S.set_pick(lvl, j);
+        return lvl + 1;
+    }
 }
 
 __device__ __forceinline__ void wide_take(const uint4 *slots, const Queue &Q, unsigned long long t,
@@ -390,13 +409,9 @@ __global__ void __launch_bounds__(TPB)
         nap = 256;
         if (busy) {
             const Mask128 g = R.gaps(L, eval, nodes);
-            bool done = apply_w(L, S, lvl, eval, last, fresh, g, leaves);
-            if (!done) {
-                fresh = false;
-                eval = advance_w(L, S, lvl, root);
-                done = eval < 0;
-            }
-            if (done) {
+            eval = apply_advance_w(L, S, lvl, eval, root, last, fresh, g, leaves);
+            fresh = false;
+            if (eval < 0) {
                 flush();
                 busy = false;
             }
