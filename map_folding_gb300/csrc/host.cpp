@@ -257,22 +257,18 @@ uint64_t sym_good_host(const uint8_t *cycle, int i, const uint8_t *edges) {
 namespace {
 
 constexpr int kMaxCentre = 25;  // 5 x 5 centre (experiments/9x9/sym_fold9.cpp:33)
-using CenterKey = std::array<uint8_t, kMaxCentre>;
 
-struct CenterKeyHash {
-    size_t operator()(const CenterKey &k) const {
-        uint64_t h = 0xcbf29ce484222325ULL;
-        for (uint8_t v : k) h = (h ^ v) * 0x100000001b3ULL;
-        return size_t(h);
+// A centre cycle packed into one integer: cell v's successor (< 25, 5 bits)
+// at bits 5v..5v+4.  Equal cycles give equal keys.
+using CentreKey = unsigned __int128;
+
+struct CentreKeyHash {
+    size_t operator()(CentreKey k) const {
+        const uint64_t lo = uint64_t(k), hi = uint64_t(k >> 64);
+        uint64_t h = lo * 0x9E3779B97F4A7C15ULL ^ (hi + 0x632BE59BD9B4E019ULL) * 0xC2B2AE3D27D4EB4FULL;
+        return size_t(h ^ (h >> 29));
     }
 };
-
-CenterKey key_of(const uint8_t *cycle, int c2) {
-    CenterKey k;
-    k.fill(255);
-    for (int i = 0; i < c2; ++i) k[i] = cycle[i];
-    return k;
-}
 
 // The eight symmetries of the c x c centre as permutations of its own
 // spiral numbering (sym_fold.cpp:316-350).
@@ -360,34 +356,37 @@ int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why, int c
     cyc[0] = 1;
     cyc[1] = 2;
     cyc[2] = 0;
+    // A cycle is new when its orbit's canonical key (the least of its 16
+    // images) has not been seen; the orbits partition the cycles, so that is
+    // the same test as looking the cycle up among all earlier orbits' members.
     const int c2 = plan.seed_i;
     auto perms = centre_symmetries(plan.c);
-    std::unordered_set<CenterKey, CenterKeyHash> seen;
-    seen.reserve(c2 > 16 ? (size_t(1) << 22) : 4096);
+    std::unordered_set<CentreKey, CentreKeyHash> seen;
+    seen.reserve(c2 > 16 ? (size_t(1) << 20) : 4096);
     plan.center_cases = 0;
     sym_expand(cyc, 3, plan.seed_i, edges, [&](const uint8_t *cy) {
         ++plan.center_cases;
-        if (seen.count(key_of(cy, c2))) return true;
-        std::array<CenterKey, 16> orbit;
+        std::array<CentreKey, 16> orbit;
         int orbit_len = 0;
+        // The image under a symmetry maps perm[u] to perm[cy[u]]; the
+        // reversed stack is its inverse (the centre is one cycle over all c2
+        // cells), mapping perm[cy[u]] to perm[u].  Both keys in one pass.
         for (const auto &perm : perms) {
-            uint8_t img[kSymCells], rev[kSymCells];
-            std::memcpy(img, cy, kSymCells);
-            for (int v = 0; v < c2; ++v) img[perm[v]] = perm[cy[v]];
-            std::memcpy(rev, img, kSymCells);
-            int v = 0;
-            do {
-                rev[img[v]] = uint8_t(v);
-                v = img[v];
-            } while (v != 0);
-            orbit[orbit_len++] = key_of(img, c2);
-            orbit[orbit_len++] = key_of(rev, c2);
+            CentreKey img = 0, rev = 0;
+            for (int u = 0; u < c2; ++u) {
+                const int pu = perm[u], pc = perm[cy[u]];
+                img |= CentreKey(pc) << (5 * pu);
+                rev |= CentreKey(pu) << (5 * pc);
+            }
+            orbit[orbit_len++] = img;
+            orbit[orbit_len++] = rev;
         }
+        const CentreKey canon = *std::min_element(orbit.begin(), orbit.begin() + orbit_len);
+        if (!seen.insert(canon).second) return true;
         std::sort(orbit.begin(), orbit.begin() + orbit_len);
         const int distinct = int(std::unique(orbit.begin(), orbit.begin() + orbit_len) - orbit.begin());
         plan.reps.insert(plan.reps.end(), cy, cy + kSymCells);
         plan.rep_mult.push_back(uint64_t(distinct));
-        seen.insert(orbit.begin(), orbit.begin() + distinct);
         return true;
     });
     plan.reduced_all = plan.rep_mult.size();
