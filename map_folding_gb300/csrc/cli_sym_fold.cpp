@@ -237,6 +237,18 @@ int main(int argc, char **argv) {
             mf_sym_plan_destroy(plan);
             return 0;
         }
+        // sym_fold.cpp:539-542: the streaming solver reads MF_QUEUE_SIZE (its
+        // host case queue's bound; nothing to size here) and rejects bad text.
+        if (stream) {
+            if (const char *q = std::getenv("MF_QUEUE_SIZE")) {
+                unsigned long long ignored = 0;
+                if (!parse_size(q, ignored)) {
+                    std::fprintf(stderr, "Invalid MF_QUEUE_SIZE: %s\n", q);
+                    mf_sym_plan_destroy(plan);
+                    return 2;
+                }
+            }
+        }
         const int rc = mf_sym_plan_solve(plan, max_cases, start_case, mode, nullptr, answer, &st);
         mf_sym_plan_destroy(plan);
         if (rc != MF_OK) {

@@ -169,3 +169,18 @@ def test_sym_fold_cli_setup_only(engine, golden):
     assert int(r.stdout.strip()) == golden["sym_setup"]["7x7_d24"]
     assert "center_cases=76" in r.stderr and "reduced_cases=11" in r.stderr
     assert "expanded_cases=433131" in r.stderr and "setup_only=1" in r.stderr
+
+
+def test_sym_fold_cli_queue_size_checked_in_stream_mode(engine):
+    """sym_fold.cpp:539-542: the streaming solver parses MF_QUEUE_SIZE after
+    the setup lines and exits 2 on bad text (the reference binary prints the
+    same four stderr lines)."""
+    import os
+    env = dict(os.environ, MF_STREAM_CASES="1", MF_QUEUE_SIZE="abc")
+    r = _cli("sym_fold", 7, 1, 10, 0, env=env)
+    assert r.returncode == 2
+    assert r.stderr.splitlines() == ["center_cases=76", "reduced_cases=11",
+                                     "stream_seed_cases=11 stream_from=9 stream_to=24",
+                                     "Invalid MF_QUEUE_SIZE: abc"]
+    env = dict(os.environ, MF_SETUP_ONLY="1", MF_QUEUE_SIZE="abc")  # not read before solving
+    assert _cli("sym_fold", 7, 1, env=env).returncode == 0
