@@ -158,11 +158,11 @@ int main(int argc, char **argv) {
         if (!std::getenv("MF_EXPANDED_N") && n >= 7) expanded_n = std::max(24, c * c);
 #endif
         const int c2 = c * c;
-        if (n >= 7 && (expanded_n < c2 || expanded_n > n * n)) {
-            std::fprintf(stderr, "MF_EXPANDED_N must be between %d and %ld\n", c2, n * n);
-            return 1;
-        }
-        opts.expanded_n = n >= 7 ? expanded_n : 0;
+        // The reference reports the centre before it checks MF_EXPANDED_N
+        // (sym_fold.cpp:703-724): on a bad depth, set up the centre alone,
+        // print its lines, then the error.
+        const bool bad_expanded = n >= 7 && (expanded_n < c2 || expanded_n > n * n);
+        opts.expanded_n = n >= 7 ? (bad_expanded ? c2 : expanded_n) : 0;
         mf_sym_plan *plan = nullptr;
         if (mf_sym_plan_create_ex(int32_t(n), &opts, &plan) != MF_OK) {
             std::fprintf(stderr, "error: %s\n", mf_last_error());
@@ -187,6 +187,11 @@ int main(int argc, char **argv) {
         std::fprintf(stderr, "center_cases=%llu\n", (unsigned long long)centers);
         std::fprintf(stderr, "reduced_cases=%llu\n", (unsigned long long)reduced);
 #endif
+        if (bad_expanded) {
+            std::fprintf(stderr, "MF_EXPANDED_N must be between %d and %ld\n", c2, n * n);
+            mf_sym_plan_destroy(plan);
+            return 1;
+        }
         if (n >= 7) {
             if (stream)
                 std::fprintf(stderr, "stream_seed_cases=%llu stream_from=%d stream_to=%d\n", seeds, c2,
