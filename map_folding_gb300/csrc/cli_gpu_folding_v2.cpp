@@ -62,8 +62,10 @@ int main(int argc, char **argv) {
         std::fprintf(stderr, "Invalid max_states: %s\n", argv[8]);
         return 2;
     }
-    if (grid < 1 || grid > 8) {
-        std::fprintf(stderr, "grid must be between 1 and 8\n");
+    // gpu_folding_v2.cu:594-607 (MAX_GRID 9); the engine's Lunnon search
+    // holds at most 64 leaves, so a 9x9 grid is refused after these checks.
+    if (grid < 1 || grid > 9) {
+        std::fprintf(stderr, "grid must be between 1 and 9\n");
         return 1;
     }
     const long n = grid * grid;
@@ -74,6 +76,11 @@ int main(int argc, char **argv) {
     if (batch < 1 || tpb < 1 || bpsm < 1 || queued < 1) {
         std::fprintf(stderr,
                      "batch_size, threads_per_block, blocks_per_sm, and max_queued_batches must be positive\n");
+        return 1;
+    }
+    if (n > 64) {
+        std::fprintf(stderr, "a %ldx%ld map has %ld leaves; this engine counts maps of up to 64\n",
+                     grid, grid, n);
         return 1;
     }
     const auto t0 = std::chrono::steady_clock::now();

@@ -63,3 +63,33 @@ def test_sym_fold9_matches_reference_binary(engine, args, env):
     if not ref.exists():
         pytest.skip("reference sym_fold9 not built here")
     assert _run(mfbuild.BIN / "sym_fold9", args, env) == _run(ref, args, env)
+
+
+# Paths of the reference's CUDA drivers that end before any CUDA call.
+GPU_FOLDING_CASES = [[], [5], [9, 5], [10, 3]]
+GPU_FOLDING_V2_CASES = [[], [6], ["x", 18], [6, "y"], [10, 18], [0, 5], [6, 0], [6, 37],
+                        [6, 18, 0], [6, 18, 5000, 0], [6, 18, 5000, 128, 8, 4, 0],
+                        [6, 18, 5000, 128, 8, 4, 8, "q"], [6, 18, 1, 2, 3, 4, 5, 6, 7]]
+
+
+@pytest.mark.parametrize("args", GPU_FOLDING_CASES)
+def test_gpu_folding_errors_match_reference_binary(engine, args):
+    from map_folding_gb300 import build as mfbuild
+
+    ref = REF / "gpu_folding"
+    if not ref.exists():
+        pytest.skip("reference gpu_folding not built here")
+    ours = _run(mfbuild.BIN / "gpu_folding", args, {})
+    theirs = _run(ref, args, {})
+    # usage text names "./gpu_folding" literally in both
+    assert ours == theirs
+
+
+@pytest.mark.parametrize("args", GPU_FOLDING_V2_CASES)
+def test_gpu_folding_v2_errors_match_reference_binary(engine, args):
+    from map_folding_gb300 import build as mfbuild
+
+    ref = REF / "gpu_folding_v2"
+    if not ref.exists():
+        pytest.skip("reference gpu_folding_v2 not built here")
+    assert _run(mfbuild.BIN / "gpu_folding_v2", args, {}) == _run(ref, args, {})
