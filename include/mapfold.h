@@ -171,7 +171,9 @@ typedef struct {
  * in the same order). */
 int32_t mf_sym_plan_create_ex(int32_t n, const mf_sym_plan_options *opts, mf_sym_plan **out);
 void mf_sym_plan_destroy(mf_sym_plan *plan);
-/* Representatives before expansion and their orbit sizes. */
+/* Board side, first searched cell (the expanded depth), centre cycles
+ * enumerated, centre representatives (before any seed slice) and the plan's
+ * number of cases.  Any output may be NULL. */
 int32_t mf_sym_plan_info(const mf_sym_plan *plan, int32_t *n, int32_t *start_i,
                          uint64_t *center_cases, uint64_t *reduced_cases,
                          uint64_t *total_cases);
@@ -199,9 +201,12 @@ uint64_t mf_sym_workspace_bytes(const mf_batch_config *cfg);
 
 /* Batched GPU count: one persistent work-stealing kernel over all cases,
  * splitting heavy subtrees on the device.  Same outputs as
- * mf_sym_count_cases.  d_workspace must hold mf_sym_workspace_bytes(cfg)
- * bytes; *d_status (optional, device uint32[4]) receives {error flag,
- * tasks run, splits, 0}.
+ * mf_sym_count_cases.  d_workspace (256-byte aligned) must hold
+ * mf_sym_workspace_bytes(cfg) bytes.  The launch is asynchronous on
+ * `stream`; once it has completed, the workspace's first 64 bytes hold the
+ * run's header: uint64 split items at byte 16, uint64 work items run at
+ * byte 32, uint32 error flag at byte 40 (non-zero: a malformed case was
+ * seen and the kernel stopped early, the counts are not valid).
  * Replaces: the same reference lines as mf_sym_count_cases; the reference
  * balances only across host threads (sym_fold.cpp:456-488). */
 int32_t mf_sym_count_cases_batched(int32_t n, int32_t start_i, int32_t stop_i,
