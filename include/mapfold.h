@@ -331,11 +331,15 @@ typedef struct {
 } mf_request_info;
 
 /* Starts a server on the current device: a persistent kernel that keeps
- * running while requests come and go.  A request is admitted as soon as a
- * slot and enough unit-arena memory are free; its units then start on
- * whichever lanes free up first, alongside the requests already running,
- * and its subtrees share the one split-item ring.  No reference counterpart:
- * the reference runs one chunk per process or container (modal_sym.py:88-137). */
+ * running while requests come and go.  A request needs a free slot and
+ * enough unit-arena memory.  Small requests (at most a quarter of the
+ * resident lanes' worth of units) are admitted at once; large ones first
+ * come first served, the next only once the running large ones leave 1/8
+ * of the lanes idle.  Admitted units start on whichever lanes free up,
+ * alongside the requests already running, and all subtrees share one
+ * split-item ring, where the oldest running request keeps a stock for lanes
+ * that free up.  No reference counterpart: the reference runs one chunk per
+ * process or container (modal_sym.py:88-137). */
 int32_t mf_server_create(const mf_server_config *cfg, mf_server **out);
 /* Submit sym_fold cases [start_case, start_case + max_cases) of an n x n
  * map at MF_EXPANDED_N = expanded_n; the result is what `sym_fold` prints
