@@ -400,6 +400,17 @@ def run_lunnon(args):
             count = min(len(a), int(count * max(2.0, 10.0 / max(el, 1e-3))))
         cpu = {"value": w.nodes / el, "unit": "nodes/s", "cores": threads, "kind": "port",
                "sample": f"first {count} of {len(a)} 6x6 depth-18 prefix states ({el:.2f} s)"}
+        # mf.c single-threaded, as the reference runs rectangles, strips and
+        # 3-D maps: the oracle's restatement on one shape of each kind.
+        single_nodes, single_s = 0, 0.0
+        for dims in ((4, 6), (1, 20), (2, 2, 5)):
+            t0 = time.perf_counter()
+            c, w1 = oracle.lunnon_count(dims)
+            single_s += time.perf_counter() - t0
+            single_nodes += w1.nodes
+            assert c == golden["x".join(map(str, dims))], dims
+        cpu["single_thread"] = {"value": single_nodes / single_s, "unit": "nodes/s", "cores": 1,
+                                "kind": "port", "sample": f"4x6, 1x20, 2x2x5 whole ({single_s:.2f} s)"}
     line = {"metric": "Lunnon DFS nodes/s over configs 1-2 (5x5@15, 6x6@18, 20 rectangles, strips 8..20)",
             "cpu_baseline": cpu,
             "value": tot_nodes / tot_b, "unit": "nodes/s", "ms_per_step": 1e3 * tot_b,
