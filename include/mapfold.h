@@ -223,20 +223,6 @@ int32_t mf_sym_plan_solve(const mf_sym_plan *plan, uint64_t max_cases, uint64_t 
                           int32_t mode, const mf_batch_config *cfg, uint64_t *answer_lo_hi,
                           mf_run_stats *stats);
 
-/* Progress of the batched (or 128-bit) sym count that another host thread
- * is running through mf_sym_plan_solve / mf_sym_solve, for a progress
- * printer polling while that thread waits.  *running = 1 while such a count
- * is on the device (0 otherwise, and nothing else is written), *units = its
- * cases, *started = cases handed to lanes so far, *finished = a lower bound
- * on the cases whose whole search has ended (finished work items minus the
- * split items made; it may step back while a tail is split up, so a printer
- * keeps the largest value it has seen).  One 64-byte device-to-host copy on
- * a private non-blocking stream; safe from any thread, no allocation.
- * Replaces: the `completed` counter of sym_fold.cpp's progress threads
- * (:442-454, :574-589). */
-int32_t mf_sym_progress(int32_t *running, uint64_t *units, uint64_t *started,
-                        uint64_t *finished);
-
 /* MF_COST_DEPTH / MF_SORT_CASES of the materialized mode: score every case
  * of the plan by its number of completions `cost_depth` cells further
  * (counted on the GPU; min, max and the uint128 total come back) and, when

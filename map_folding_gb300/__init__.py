@@ -20,7 +20,6 @@ from .api import (  # noqa: F401
     solve_cases,
     sym_edges,
     sym_fold,
-    sym_progress,
     sym_sort_order,
     sym_workspace_bytes,
 )

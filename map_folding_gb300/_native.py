@@ -117,7 +117,6 @@ SIGNATURES = {
     "mf_sym_workspace_bytes": ([_p], _u64),
     "mf_sym_count_cases_batched": ([_i32, _i32, _i32, _p, _u64, _p, _p, _p, _u64, _p, _p], _i32),
     "mf_sym_plan_solve": ([_p, _u64, _u64, _i32, _p, _p, _p], _i32),
-    "mf_sym_progress": ([ctypes.POINTER(_i32), _pu64, _pu64, _pu64], _i32),
     "mf_sym_plan_score": ([_p, _i32, _i32, _i32, _p, _pu64, _pu64, _p, _p], _i32),
     "mf_sym_sort_order": ([_p, _p, _u64, _i32, _p], _i32),
     "mf_sym_plan_block_costs": ([_p, _u64, _u64, _i32, _u64, _i32, _p, _p], _i32),

@@ -312,21 +312,6 @@ class SymPlan:
         return _u128(ans), st
 
 
-def sym_progress() -> dict | None:
-    """Progress of the batched sym count another thread is running (ctypes
-    releases the GIL during a solve): {"units", "started", "finished"}, with
-    "finished" a lower bound on cases done; None when no count is on the
-    device.  The counters behind sym_fold.cpp's progress lines (:442-454,
-    :574-589)."""
-    running = ctypes.c_int32(0)
-    units, started, finished = ctypes.c_uint64(0), ctypes.c_uint64(0), ctypes.c_uint64(0)
-    check(_native.load().mf_sym_progress(ctypes.byref(running), ctypes.byref(units),
-                                         ctypes.byref(started), ctypes.byref(finished)))
-    if not running.value:
-        return None
-    return {"units": units.value, "started": started.value, "finished": finished.value}
-
-
 def sym_sort_order(scores, mults, ascending: bool = False) -> np.ndarray:
     """The reference's cost order (sym_fold.cpp:297-310) on the host:
     indices of the cases sorted by score, ties by multiplier."""

@@ -152,66 +152,6 @@ struct Timer {
 
 using u128 = unsigned __int128;
 
-// The batched sym count on the device right now, for mf_sym_progress.  The
-// solving thread arms it before its launch and disarms it when the count's
-// stream is done; a reader copies the queue header under the same lock, so
-// no copy reads a workspace that has been released or reused.
-struct ProgressSlot {
-    std::mutex mu;
-    void *d_hdr = nullptr;  // QueueHeader of the running count
-    uint64_t units = 0;
-    int device = -1;
-    cudaStream_t stream = nullptr;  // non-blocking: never waits for the count
-    cudaEvent_t ready = nullptr;    // on the count's stream, after the header is zeroed
-    QueueHeader *h_snap = nullptr;  // pinned snapshot
-};
-ProgressSlot g_progress;
-
-// Called by the solving thread before its launch on `s` (the stream, event
-// and pinned snapshot are made here, ahead of the kernel, once per process
-// or device).  The header is zeroed on `s` and `ready` recorded behind it, so
-// a reader never sees the previous count's figures.
-bool arm_progress(void *d_hdr, uint64_t units, cudaStream_t s) {
-    std::lock_guard<std::mutex> lock(g_progress.mu);
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return false;
-    if (g_progress.device != dev) {
-        if (g_progress.stream) cudaStreamDestroy(g_progress.stream);
-        if (g_progress.ready) cudaEventDestroy(g_progress.ready);
-        g_progress.stream = nullptr;
-        g_progress.ready = nullptr;
-        g_progress.device = -1;
-        if (cudaStreamCreateWithFlags(&g_progress.stream, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&g_progress.ready, cudaEventDisableTiming) != cudaSuccess)
-            return false;
-        g_progress.device = dev;
-    }
-    if (!g_progress.h_snap &&
-        cudaHostAlloc(reinterpret_cast<void **>(&g_progress.h_snap), sizeof(QueueHeader),
-                      cudaHostAllocPortable) != cudaSuccess) {
-        g_progress.h_snap = nullptr;
-        return false;
-    }
-    if (cudaMemsetAsync(d_hdr, 0, sizeof(QueueHeader), s) != cudaSuccess ||
-        cudaEventRecord(g_progress.ready, s) != cudaSuccess)
-        return false;
-    g_progress.d_hdr = d_hdr;
-    g_progress.units = units;
-    return true;
-}
-
-struct ProgressArm {
-    bool on;
-    ProgressArm(void *d_hdr, uint64_t units, cudaStream_t s, bool want)
-        : on(want && arm_progress(d_hdr, units, s)) {}
-    ~ProgressArm() {
-        if (!on) return;
-        std::lock_guard<std::mutex> lock(g_progress.mu);
-        g_progress.d_hdr = nullptr;
-        g_progress.units = 0;
-    }
-};
-
 }  // namespace
 }  // namespace mf
 
@@ -976,8 +916,6 @@ int count_cases_host(int n, int start_i, int stop_i, const uint8_t *h_cycles, ui
     cudaEventRecord(th.a, s);
     MF_TRY_CUDA(cudaMemcpyAsync(d_cycles, h_cycles, in_bytes, cudaMemcpyHostToDevice, s));
     MF_TRY_CUDA(cudaMemsetAsync(d_counts + num, 0, 8, s));
-    // Visible to mf_sym_progress until this function returns.
-    ProgressArm progress(d_work, num, s, mode == 1);
     cudaEventRecord(th.b, s);
     cudaEventRecord(tk.a, s);
     if (wide)
@@ -1147,42 +1085,6 @@ int32_t mf_sym_plan_solve(const mf_sym_plan *plan, uint64_t max_cases, uint64_t 
     answer_lo_hi[0] = uint64_t(answer);
     answer_lo_hi[1] = uint64_t(answer >> 64);
     st->total_s = now_seconds() - t0;
-    return MF_OK;
-}
-
-int32_t mf_sym_progress(int32_t *running, uint64_t *units, uint64_t *started, uint64_t *finished) {
-    clear_error();
-    if (running) *running = 0;
-    std::lock_guard<std::mutex> lock(g_progress.mu);
-    if (!g_progress.d_hdr) return MF_OK;
-    int old = -1;
-    cudaGetDevice(&old);
-    if (old != g_progress.device) cudaSetDevice(g_progress.device);
-    QueueHeader h{};
-    cudaError_t e = cudaEventQuery(g_progress.ready);
-    if (e == cudaErrorNotReady) {
-        e = cudaSuccess;  // the header is not zeroed yet: nothing has started
-    } else if (e == cudaSuccess) {
-        e = cudaMemcpyAsync(g_progress.h_snap, g_progress.d_hdr, sizeof(QueueHeader),
-                            cudaMemcpyDeviceToHost, g_progress.stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(g_progress.stream);
-        if (e == cudaSuccess) h = *g_progress.h_snap;
-    }
-    if (old >= 0 && old != g_progress.device) cudaSetDevice(old);
-    if (e != cudaSuccess) {
-        set_error("reading the running count's progress failed: %s", cudaGetErrorString(e));
-        return MF_ERR_CUDA;
-    }
-    const uint64_t u = g_progress.units;
-    // init_next counts units fetched ahead of their start as well.
-    const uint64_t s = std::min<uint64_t>(h.init_next, u);
-    // Every unfinished case holds at least one unfinished work item, so the
-    // finished items minus the split items made bound the finished cases.
-    const uint64_t f = h.completed > h.spawn_tail ? std::min<uint64_t>(h.completed - h.spawn_tail, s) : 0;
-    if (running) *running = 1;
-    if (units) *units = u;
-    if (started) *started = s;
-    if (finished) *finished = f;
     return MF_OK;
 }
 

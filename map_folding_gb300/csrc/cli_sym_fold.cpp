@@ -14,11 +14,9 @@
 // (sym_fold9.cpp:963-1198); counting past cell 63 uses the 128-bit kernel.
 #include <algorithm>
 #include <chrono>
-#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <mutex>
 #include <string>
 #include <thread>
 
@@ -54,60 +52,6 @@ bool parse_size(const char *text, unsigned long long &out) {
     out = std::strtoull(text, &end, 10);
     return *text != '\0' && *end == '\0';
 }
-
-// The reference's progress lines, every 5 s while the count runs
-// (sym_fold.cpp:442-454 materialized, :574-589 streaming), from the device's
-// counters through mf_sym_progress.  `completed` is the largest lower bound
-// seen so far; before the device starts (host-side case selection) the
-// streaming line shows nothing selected and the producer not done.
-class ProgressPrinter {
-  public:
-    ProgressPrinter(bool stream, unsigned long long planned)
-        : stream_(stream), planned_(planned), start_(Clock::now()), thread_([this] { run(); }) {}
-    ~ProgressPrinter() {
-        {
-            std::lock_guard<std::mutex> lock(mu_);
-            done_ = true;
-        }
-        cv_.notify_all();
-        thread_.join();
-    }
-
-  private:
-    void run() {
-        std::unique_lock<std::mutex> lock(mu_);
-        unsigned long long completed = 0, units = 0;
-        bool seen = false;
-        while (!done_) {
-            if (cv_.wait_for(lock, std::chrono::seconds(5), [this] { return done_; })) break;
-            int32_t running = 0;
-            uint64_t u = 0, started = 0, finished = 0;
-            if (mf_sym_progress(&running, &u, &started, &finished) == MF_OK && running) {
-                seen = true;
-                units = u;
-                completed = std::max<unsigned long long>(completed, finished);
-            }
-            const double el = since(start_);
-            const double rate = el > 0.0 ? double(completed) / el : 0.0;
-            if (stream_)
-                std::fprintf(stderr,
-                             "stream selected=%llu completed=%llu producer_done=%d rate=%g/s "
-                             "elapsed_s=%g\n",
-                             units, completed, seen ? 1 : 0, rate, el);
-            else
-                std::fprintf(stderr, "progress=%llu/%llu rate=%g/s elapsed_s=%g\n", completed,
-                             seen ? units : planned_, rate, el);
-        }
-    }
-
-    const bool stream_;
-    const unsigned long long planned_;
-    const Clock::time_point start_;
-    std::mutex mu_;
-    std::condition_variable cv_;
-    bool done_ = false;
-    std::thread thread_;  // last: starts once the members above exist
-};
 
 void usage(const char *exe) {
     std::fprintf(stderr, "Usage: %s n [threads] [max_cases] [start_case]\nExample: %s 6 12\n", exe,
@@ -310,13 +254,7 @@ int main(int argc, char **argv) {
                 }
             }
         }
-        unsigned long long planned = total > start_case ? total - start_case : 0;
-        if (max_cases && max_cases < planned) planned = max_cases;
-        int rc = MF_OK;
-        {
-            ProgressPrinter printer(stream, planned);
-            rc = mf_sym_plan_solve(plan, max_cases, start_case, mode, nullptr, answer, &st);
-        }
+        const int rc = mf_sym_plan_solve(plan, max_cases, start_case, mode, nullptr, answer, &st);
         mf_sym_plan_destroy(plan);
         if (rc != MF_OK) {
             std::fprintf(stderr, "error: %s\n", mf_last_error());

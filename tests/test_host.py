@@ -124,11 +124,6 @@ def test_solve_cases_status_codes(engine):
     assert engine.solve_cases(5, 3, 26, b"", 0)[2] == 2
 
 
-def test_sym_progress_idle(engine):
-    # Nothing counting: reported as idle without touching a device.
-    assert engine.sym_progress() is None
-
-
 def _cli(name, *args, env=None):
     from map_folding_gb300 import build
 
