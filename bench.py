@@ -126,9 +126,9 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def cpu_sample_cases(budget_s: float = 12.0):
-    """A bounded prefix of the 7x7 cases for the CPU legs (about budget_s of
-    work on all host cores)."""
+def all_cases_7x7():
+    """The 7x7 depth-24 case list in emission order, from the oracle; the CPU
+    legs time a bounded prefix of it (time_cpu)."""
     from oracle import oracle
 
     cyc, mult = oracle.sym_expand(N, EXPANDED_N, 0, 0)
@@ -159,7 +159,7 @@ def run_reference(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    cases, mults = cpu_sample_cases()
+    cases, mults = all_cases_7x7()
     rate, sample, el, count = time_cpu(cases, mults, threads, target_s=8.0)
     from oracle import oracle
 
