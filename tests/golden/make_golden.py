@@ -4,6 +4,7 @@ solvers, built from source by `make -C oracle ref` into oracle/_ref/.
     python tests/golden/make_golden.py          # needs oracle/_ref/{mf,mf_fast,sym_fold}
     python tests/golden/make_golden.py --cost   # refresh only the cost-order vectors
     python tests/golden/make_golden.py --sym9   # refresh only the sym_fold9 (9x9) vectors
+    python tests/golden/make_golden.py --high-dim  # refresh only the 3- to 5-D Lunnon maps
 
 Every value in the output was printed by an unmodified reference binary on
 this machine; published values quoted in the reference's documents are kept
@@ -138,7 +139,29 @@ def lunnon_jobs():
         jobs.append((f"2x2x{k}", [REF / "mf", 2, 2, k]))
     jobs.append(("1x1", [REF / "mf", 1, 1]))
     jobs.append(("2x3x4", [REF / "mf", 2, 3, 4]))
+    jobs.extend(high_dim_jobs())
     return jobs
+
+
+# Maps of three to five dimensions beyond the 2x2xk family (mf.c takes any
+# number of dimensions); each runs in a few seconds at most.
+HIGH_DIM_SHAPES = [(2, 2, 6), (3, 3, 3), (2, 2, 2, 2), (2, 2, 2, 3), (2, 2, 2, 2, 2)]
+
+
+def high_dim_jobs():
+    return [("x".join(map(str, d)), [REF / "mf", *d]) for d in HIGH_DIM_SHAPES]
+
+
+def main_high_dim():
+    """Refresh only the higher-dimensional Lunnon counts in the golden file."""
+    path = HERE / "reference_counts.json"
+    out = json.loads(path.read_text())
+    with ThreadPoolExecutor(max_workers=os.cpu_count()) as ex:
+        futs = {k: ex.submit(run, cmd) for k, cmd in high_dim_jobs()}
+        for k, f in futs.items():
+            out["lunnon"][k] = int(f.result())
+    path.write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
+    print(json.dumps({k: out["lunnon"][k] for k in futs}, indent=1, sort_keys=True))
 
 
 def prefix_jobs():
@@ -233,5 +256,7 @@ if __name__ == "__main__":
         main_cost()
     elif "--sym9" in sys.argv:
         main_sym9()
+    elif "--high-dim" in sys.argv:
+        main_high_dim()
     else:
         main()

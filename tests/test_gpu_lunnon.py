@@ -13,7 +13,8 @@ def shape_of(key):
 SMALL_SHAPES = ["2x2", "2x3", "2x4", "2x5", "2x6", "3x3", "3x4", "3x5", "3x6", "4x4", "4x5",
                 "4x6", "5x5", "5x6", "1x8", "1x9", "1x10", "1x11", "1x12", "1x13", "1x14",
                 "1x15", "1x16", "1x17", "1x18", "1x19", "1x20", "2x2x1", "2x2x2", "2x2x3",
-                "2x2x4", "2x2x5", "1x1", "2x3x4"]
+                "2x2x4", "2x2x5", "1x1", "2x3x4", "2x2x6", "3x3x3", "2x2x2x2", "2x2x2x3",
+                "2x2x2x2x2"]
 
 
 @pytest.mark.parametrize("key", SMALL_SHAPES)

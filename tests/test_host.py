@@ -40,6 +40,9 @@ def test_exports_match_nm(engine):
 @pytest.mark.parametrize("dims,depth", [
     ((5, 5), 15), ((4, 4), 8), ((2, 3), 3), ((1, 12), 6), ((2, 2, 3), 5), ((3, 5), 0),
     ((2, 2), 4), ((4, 6), 12), ((2, 2, 5), 9), ((1, 1), 1), ((3, 3), 9), ((1, 20), 10),
+    # up to six dimensions and the 64-leaf limit
+    ((2, 2, 2, 2), 10), ((2, 2, 2, 2, 2), 14), ((3, 3, 3), 14), ((4, 4, 4), 12), ((8, 8), 10),
+    ((1, 64), 16), ((2, 2, 2, 2, 2, 2), 12),
 ])
 def test_prefix_states_match_oracle(engine, orc, dims, depth):
     plan = engine.LunnonPlan(dims)
