@@ -94,3 +94,39 @@ def test_gpu_folding_function(engine, cuda, golden):
     assert total == golden["lunnon"]["5x5"]
     states, total = engine.gpu_folding(4, 5, mode="plain", dims=(3, 5))
     assert total == golden["lunnon"]["3x5"]
+
+
+def test_gpu_folding_v2_cli(engine, cuda, golden, orc):
+    """bin/gpu_folding_v2 on its counting path (gpu_folding_v2.cu:610-699):
+    the decimal count alone on stdout, the key=value lines on stderr, and
+    max_states stopping after the first states of the emission order."""
+    import subprocess
+
+    from map_folding_gb300 import build
+
+    def run(*args):
+        return subprocess.run([str(build.BIN / "gpu_folding_v2"), *map(str, args)],
+                              capture_output=True, text=True, timeout=300)
+
+    r = run(5, 15)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout == f"{golden['lunnon']['5x5']}\n"
+    err = r.stderr.splitlines()
+    assert err[0] == ("gpus=1 batch_size=100000 threads_per_block=128 blocks_per_sm=8 "
+                      "max_queued_batches=8 max_states=0")
+    assert err[1].startswith("grid=5 depth=15 states=13416 collect_s=")
+    assert err[2].startswith("solve_s=") and " total_s=" in err[2]
+
+    # the README's example invocation
+    r = run(6, 18, 5000, 128, 8, 4, 8, 0)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout == f"{golden['published']['squares']['6']}\n"
+    assert "grid=6 depth=18 states=112024 collect_s=" in r.stderr
+
+    # max_states: the subtrees of the first 1000 prefix states only
+    a, b, _ = orc.lunnon_collect((5, 5), 15)
+    want, _, _ = orc.lunnon_resume_many((5, 5), 16, a[:1000], b[:1000], threads=8)
+    r = run(5, 15, 5000, 128, 8, 1, 8, 1000)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout == f"{want}\n"
+    assert "grid=5 depth=15 states=1000 collect_s=" in r.stderr
