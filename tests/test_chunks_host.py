@@ -65,3 +65,27 @@ def test_sweep_resumes_without_repeating_chunks(tmp_path, monkeypatch):
     assert calls == [0, 10, 20, 30, 40]
     summary = chunks.validate(str(out), total_cases=50, chunk_size=10)
     assert summary["complete"] and summary["unique_sum"] == str(0 + 10 + 20 + 30 + 40)
+
+
+def _fixture():
+    from pathlib import Path
+
+    return json.loads((Path(__file__).resolve().parent / "golden" /
+                       "jsonl_summaries.json").read_text())
+
+
+def test_summaries_match_the_reference_function(tmp_path):
+    """summarize_jsonl against the reference's own modal_sym.py:36-77 run on
+    the same files (tests/golden/make_jsonl_summaries.py)."""
+    for case in _fixture()["summaries"]:
+        p = tmp_path / f"{case['name']}.jsonl"
+        if case["jsonl"] is not None:
+            p.write_text(case["jsonl"], encoding="utf-8")
+        got = chunks.summarize_jsonl(p, case["total_cases"], case["chunk_size"])
+        got["path"] = p.name
+        assert got == case["summary"], case["name"]
+
+
+def test_parse_result_matches_the_reference_function():
+    for case in _fixture()["parse_result"]:
+        assert chunks.parse_result(case["stdout"]) == case["result"], case["stdout"]
