@@ -128,6 +128,7 @@ int main(int argc, char **argv) {
     } else {
         mf_sym_plan_options opts{};
         int c = (n % 2 == 0) ? 4 : 3;
+        std::string bad_seed;  // reported after the centre lines, as the reference does
 #ifdef MF_SYM_FOLD9
         // sym_fold9.cpp:969-981.
         if (n >= 9) c = 5;
@@ -141,19 +142,18 @@ int main(int argc, char **argv) {
         opts.center_n = c;
         unsigned long long seed_start = 0, seed_count = 0;
         const char *seed_start_text = std::getenv("MF_SEED_START");
+        // sym_fold9.cpp:1071-1086 parses the slice after the centre setup and
+        // exits 2 on bad text there.
         if (seed_start_text) {
-            if (!parse_size(seed_start_text, seed_start)) {
-                std::fprintf(stderr, "Invalid MF_SEED_START: %s\n", seed_start_text);
-                return 2;
+            const char *count_text = std::getenv("MF_SEED_COUNT");
+            if (!parse_size(seed_start_text, seed_start))
+                bad_seed = std::string("Invalid MF_SEED_START: ") + seed_start_text;
+            else if (count_text && !parse_size(count_text, seed_count))
+                bad_seed = std::string("Invalid MF_SEED_COUNT: ") + count_text;
+            if (bad_seed.empty()) {
+                opts.seed_start = seed_start;
+                opts.seed_count = seed_count;
             }
-            if (const char *t = std::getenv("MF_SEED_COUNT")) {
-                if (!parse_size(t, seed_count)) {
-                    std::fprintf(stderr, "Invalid MF_SEED_COUNT: %s\n", t);
-                    return 2;
-                }
-            }
-            opts.seed_start = seed_start;
-            opts.seed_count = seed_count;
         }
         if (!std::getenv("MF_EXPANDED_N") && n >= 7) expanded_n = std::max(24, c * c);
 #endif
@@ -162,7 +162,7 @@ int main(int argc, char **argv) {
         // (sym_fold.cpp:703-724): on a bad depth, set up the centre alone,
         // print its lines, then the error.
         const bool bad_expanded = n >= 7 && (expanded_n < c2 || expanded_n > n * n);
-        opts.expanded_n = n >= 7 ? (bad_expanded ? c2 : expanded_n) : 0;
+        opts.expanded_n = n >= 7 ? (bad_expanded || !bad_seed.empty() ? c2 : expanded_n) : 0;
         mf_sym_plan *plan = nullptr;
         if (mf_sym_plan_create_ex(int32_t(n), &opts, &plan) != MF_OK) {
             std::fprintf(stderr, "error: %s\n", mf_last_error());
@@ -176,10 +176,15 @@ int main(int argc, char **argv) {
         std::fprintf(stderr, "center_size=%d center_cases=%llu%s\n", c, (unsigned long long)centers,
                      std::getenv("MF_CENTER_STREAM_DEDUP") ? " center_stream_dedup=1" : "");
         std::fprintf(stderr, "reduced_cases=%llu\n", (unsigned long long)reduced);
+        if (!bad_seed.empty()) {
+            std::fprintf(stderr, "%s\n", bad_seed.c_str());
+            mf_sym_plan_destroy(plan);
+            return 2;
+        }
         if (seed_start_text) {
             const unsigned long long lo = std::min<unsigned long long>(seed_start, reduced);
             const unsigned long long hi =
-                seed_count ? std::min<unsigned long long>(reduced, lo + seed_count) : reduced;
+                seed_count && seed_count < reduced - lo ? lo + seed_count : reduced;
             seeds = hi - lo;
             std::fprintf(stderr, "seed_slice_start=%llu seed_slice_count=%llu\n", seed_start, seeds);
         }

@@ -395,7 +395,8 @@ int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why, int c
     if (seed_start > 0 || seed_count > 0) {
         const uint64_t reps = plan.rep_mult.size();
         const uint64_t lo = std::min(seed_start, reps);
-        const uint64_t hi = seed_count ? std::min(reps, lo + seed_count) : reps;
+        // Saturating: a count past the end (or one that would wrap) runs to it.
+        const uint64_t hi = seed_count && seed_count < reps - lo ? lo + seed_count : reps;
         plan.reps = std::vector<uint8_t>(plan.reps.begin() + long(lo * kSymCells),
                                          plan.reps.begin() + long(hi * kSymCells));
         plan.rep_mult = std::vector<uint64_t>(plan.rep_mult.begin() + long(lo),

@@ -52,6 +52,17 @@ SYM9_CASES = [
     ([9, 1], {"MF_CENTER_N": "5", "MF_SETUP_ONLY": "1", "MF_CENTER_STREAM_DEDUP": "1",
               "MF_STREAM_CASES": "1", "MF_SEED_START": "1000", "MF_SEED_COUNT": "10"}),
     ([7, 1], {"MF_CENTER_N": "5", "MF_SETUP_ONLY": "1", "MF_EXPANDED_N": "25"}),
+    ([9, 1], {"MF_CENTER_N": "3", "MF_SETUP_ONLY": "1"}),
+    ([9, 1], {"MF_CENTER_N": "3", "MF_SETUP_ONLY": "1", "MF_EXPANDED_N": "20"}),
+    ([9, 1], {"MF_CENTER_N": "5", "MF_SETUP_ONLY": "1", "MF_EXPANDED_N": "24"}),
+    ([9, 1], {"MF_CENTER_N": "5", "MF_SETUP_ONLY": "1", "MF_STREAM_CASES": "1",
+              "MF_SEED_START": "99999999"}),
+    ([7, 1], {"MF_CENTER_N": "3", "MF_SETUP_ONLY": "1"}),
+    ([8, 1], {"MF_CENTER_N": "4", "MF_SETUP_ONLY": "1", "MF_EXPANDED_N": "20"}),
+    ([6, 1], {"MF_SETUP_ONLY": "1"}),
+    # bad slice text: reported after the centre lines, rc 2
+    ([9, 1], {"MF_CENTER_N": "5", "MF_SEED_START": "x"}),
+    ([9, 1], {"MF_CENTER_N": "5", "MF_SEED_START": "3", "MF_SEED_COUNT": "y"}),
 ]
 
 
