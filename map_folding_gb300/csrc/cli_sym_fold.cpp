@@ -269,11 +269,11 @@ int main(int argc, char **argv) {
         if (stream)
             std::fprintf(stderr, "stream selected=%llu completed=%llu producer_done=1 rate=%g/s elapsed_s=%g\n",
                          (unsigned long long)st.units, (unsigned long long)st.units,
-                         el > 0 ? st.units / el : 0.0, el);
+                         el > 0 ? double(st.units) / el : 0.0, el);
         else
             std::fprintf(stderr, "progress=%llu/%llu rate=%g/s elapsed_s=%g\n",
                          (unsigned long long)st.units, (unsigned long long)st.units,
-                         el > 0 ? st.units / el : 0.0, el);
+                         el > 0 ? double(st.units) / el : 0.0, el);
     }
     std::printf("%s\n", decimal(answer[0], answer[1]).c_str());
     std::fprintf(stderr, "n=%ld threads=%ld max_cases=%llu start_case=%llu total_s=%g\n", n, threads,

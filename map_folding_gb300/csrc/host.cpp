@@ -366,7 +366,7 @@ int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why, int c
     plan.center_cases = 0;
     sym_expand(cyc, 3, plan.seed_i, edges, [&](const uint8_t *cy) {
         ++plan.center_cases;
-        std::array<CentreKey, 16> orbit;
+        std::array<CentreKey, 16> orbit{};
         int orbit_len = 0;
         // The image under a symmetry maps perm[u] to perm[cy[u]]; the
         // reversed stack is its inverse (the centre is one cycle over all c2
