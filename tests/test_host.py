@@ -4,7 +4,6 @@ import re
 import subprocess
 from pathlib import Path
 
-import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
