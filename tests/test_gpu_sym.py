@@ -140,6 +140,22 @@ def test_solve_cases_multiplier(engine, cuda, orc):
     assert status == 0 and count == total
 
 
+def test_solve_cases_mfah_campaign(engine, cuda, orc, golden):
+    """The bounded 7x7 campaign of mfah/README.md:59-68 through solve_cases,
+    as its coordinator hands it out: the raw 14-cell prefixes in units of 64
+    (MFAH_PREFIXES_PER_UNIT), each counted to 28 cells; the units' counts
+    total 35044546."""
+    prefixes = orc.sym_raw_prefixes(7, 14)
+    total = 0
+    for k in range(0, len(prefixes), 64):
+        unit = prefixes[k:k + 64]
+        buf = engine.pack_case_buffer(unit, [1] * len(unit), 7)
+        count, nodes, status = engine.solve_cases(7, 14, 28, buf, len(unit))
+        assert status == 0
+        total += count
+    assert total == golden["published"]["mfah_7x7_d14_s28"]
+
+
 def _cli(name, *args, env=None):
     from map_folding_gb300 import build
 

@@ -91,6 +91,20 @@ def test_wasm_vectors(orc):
         assert total == v["expected"]
 
 
+def test_mfah_campaign_total(orc, golden):
+    """mfah/README.md:59-68: the bounded 7x7 campaign -- every raw prefix at
+    14 cells grown from the 3-cell cycle, counted to 28 cells -- totals
+    35044546."""
+    prefixes = orc.sym_raw_prefixes(7, 14)
+    per = orc.sym_estimate_cases(7, 14, 14, prefixes, threads=THREADS)
+    assert int(per.sum()) == golden["published"]["mfah_7x7_d14_s28"]
+    # its first unit of 64 prefixes is the WASM test's 7x7 payload
+    vecs = json.loads((ROOT / "tests" / "golden" / "wasm_vectors.json").read_text())
+    first = next(v for v in vecs["cases"] if v["n"] == 7)
+    assert (prefixes[:64] == np.array(first["prefix_bytes"], np.uint8)).all()
+    assert int(per[:64].sum()) == first["expected"]
+
+
 def test_sym_node_counts_are_consistent(orc):
     # nodes of a whole count equal the sum over its cases' subtrees plus the
     # nodes above the case depth
