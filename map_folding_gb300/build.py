@@ -83,7 +83,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         # Link to a temporary name and rename: the linker rewrites an existing
         # output in place, which would corrupt processes that have it mapped.
         tmp = LIB.with_suffix(".so.tmp")
-        _run([cc, "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-lcudart"])
+        _run([cc, "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-lcudart",
+              "-Xcompiler", "-pthread"])
         os.replace(tmp, LIB)
     for name, (src, _) in CLI_SOURCES.items():
         o = OBJ / f"cli_{name}.o"

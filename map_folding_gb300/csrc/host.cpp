@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <set>
+#include <thread>
 #include <unordered_set>
 
 #include "engine.hpp"
@@ -258,6 +259,11 @@ namespace {
 
 constexpr int kMaxCentre = 25;  // 5 x 5 centre (experiments/9x9/sym_fold9.cpp:33)
 
+size_t host_threads() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    return hw ? hw : 1;
+}
+
 // A centre cycle packed into one integer: cell v's successor (< 25, 5 bits)
 // at bits 5v..5v+4.  Equal cycles give equal keys.
 using CentreKey = unsigned __int128;
@@ -348,47 +354,74 @@ int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why, int c
     const uint8_t *edges = plan.edges.data();
 
     // Centre cycles: every cycle of the c*c centre cells (sym_fold.cpp:703-707),
-    // deduplicated as they are generated (sym_fold9.cpp:601-627 gives the same
+    // deduplicated in generation order (sym_fold9.cpp:601-627 gives the same
     // representatives in the same order as deduplicating the stored list):
     // orbit representatives under the square's symmetries and reversal of the
-    // stack, sym_fold.cpp:361-408; the multiplier is the orbit size.
+    // stack, sym_fold.cpp:361-408; the multiplier is the orbit size.  An
+    // orbit's canonical key is the least of its 16 images.
     uint8_t cyc[kSymCells] = {0};
     cyc[0] = 1;
     cyc[1] = 2;
     cyc[2] = 0;
-    // A cycle is new when its orbit's canonical key (the least of its 16
-    // images) has not been seen; the orbits partition the cycles, so that is
-    // the same test as looking the cycle up among all earlier orbits' members.
     const int c2 = plan.seed_i;
-    auto perms = centre_symmetries(plan.c);
-    std::unordered_set<CentreKey, CentreKeyHash> seen;
-    seen.reserve(c2 > 16 ? (size_t(1) << 20) : 4096);
-    plan.center_cases = 0;
-    sym_expand(cyc, 3, plan.seed_i, edges, [&](const uint8_t *cy) {
-        ++plan.center_cases;
-        std::array<CentreKey, 16> orbit{};
-        int orbit_len = 0;
-        // The image under a symmetry maps perm[u] to perm[cy[u]]; the
-        // reversed stack is its inverse (the centre is one cycle over all c2
-        // cells), mapping perm[cy[u]] to perm[u].  Both keys in one pass.
-        for (const auto &perm : perms) {
-            CentreKey img = 0, rev = 0;
-            for (int u = 0; u < c2; ++u) {
-                const int pu = perm[u], pc = perm[cy[u]];
-                img |= CentreKey(pc) << (5 * pu);
-                rev |= CentreKey(pu) << (5 * pc);
-            }
-            orbit[orbit_len++] = img;
-            orbit[orbit_len++] = rev;
-        }
-        const CentreKey canon = *std::min_element(orbit.begin(), orbit.begin() + orbit_len);
-        if (!seen.insert(canon).second) return true;
-        std::sort(orbit.begin(), orbit.begin() + orbit_len);
-        const int distinct = int(std::unique(orbit.begin(), orbit.begin() + orbit_len) - orbit.begin());
-        plan.reps.insert(plan.reps.end(), cy, cy + kSymCells);
-        plan.rep_mult.push_back(uint64_t(distinct));
+    const auto perms = centre_symmetries(plan.c);
+    // 1. Every centre cycle in DFS order (c2 bytes each; cells past c2 stay 0).
+    std::vector<uint8_t> centres;
+    sym_expand(cyc, 3, c2, edges, [&](const uint8_t *cy) {
+        centres.insert(centres.end(), cy, cy + c2);
         return true;
     });
+    const size_t count = centres.size() / size_t(c2);
+    plan.center_cases = count;
+    // 2. Canonical key and orbit size of each, on all host threads.  The
+    // image under a symmetry maps perm[u] to perm[cy[u]]; the reversed stack
+    // is its inverse (the centre is one cycle over all c2 cells), mapping
+    // perm[cy[u]] to perm[u].  Both keys in one pass.
+    std::vector<CentreKey> canon(count);
+    std::vector<uint8_t> orbit_size(count);
+    auto keys = [&](size_t lo, size_t hi) {
+        for (size_t k = lo; k < hi; ++k) {
+            const uint8_t *cy = &centres[k * size_t(c2)];
+            std::array<CentreKey, 16> orbit{};
+            int orbit_len = 0;
+            for (const auto &perm : perms) {
+                CentreKey img = 0, rev = 0;
+                for (int u = 0; u < c2; ++u) {
+                    const int pu = perm[u], pc = perm[cy[u]];
+                    img |= CentreKey(pc) << (5 * pu);
+                    rev |= CentreKey(pu) << (5 * pc);
+                }
+                orbit[orbit_len++] = img;
+                orbit[orbit_len++] = rev;
+            }
+            std::sort(orbit.begin(), orbit.begin() + orbit_len);
+            canon[k] = orbit[0];
+            orbit_size[k] =
+                uint8_t(std::unique(orbit.begin(), orbit.begin() + orbit_len) - orbit.begin());
+        }
+    };
+    const size_t workers = count < 65536 ? 1 : std::min<size_t>(host_threads(), 64);
+    if (workers <= 1) {
+        keys(0, count);
+    } else {
+        std::vector<std::thread> pool;
+        const size_t step = (count + workers - 1) / workers;
+        for (size_t lo = 0; lo < count; lo += step)
+            pool.emplace_back(keys, lo, std::min(count, lo + step));
+        for (auto &t : pool) t.join();
+    }
+    // 3. In DFS order, a cycle is a representative when its orbit's key is
+    // new: the orbits partition the cycles, so that is the same test as
+    // looking the cycle up among all earlier orbits' members.
+    std::unordered_set<CentreKey, CentreKeyHash> seen;
+    seen.reserve(count / 4 + 16);
+    for (size_t k = 0; k < count; ++k) {
+        if (!seen.insert(canon[k]).second) continue;
+        const size_t at = plan.reps.size();
+        plan.reps.resize(at + kSymCells, 0);
+        std::memcpy(&plan.reps[at], &centres[k * size_t(c2)], size_t(c2));
+        plan.rep_mult.push_back(orbit_size[k]);
+    }
     plan.reduced_all = plan.rep_mult.size();
     // sym_fold9.cpp:1071-1088: MF_SEED_START / MF_SEED_COUNT slice the
     // representatives; case indices then run within the slice.
