@@ -210,3 +210,33 @@ def test_concurrent_host_threads_match_sequential(engine, cuda, golden):
     want = [golden["sym"]["7x7_d24_first2000"], golden["sym"]["7x7_d24_300000+500"],
             golden["lunnon"]["4x5"], golden["published"]["squares"]["6"]] * 3
     assert got == want
+
+
+def test_empty_and_ragged_chunks(engine, cuda, golden):
+    """Chunk edge cases (sym_fold.cpp:416-426, 536-545; modal_sym.py:166-172): a chunk
+    at or past the last case counts 0, a chunk running past the end stops
+    there, and chunks that tile the cases sum to the whole count."""
+    plan = engine.SymPlan(6)
+    try:
+        total = plan.total_cases
+        assert plan.solve(10, total)[0] == 0
+        assert plan.solve(0, total + 5)[0] == 0
+        head, _ = plan.solve(500, 0)
+        tail, st = plan.solve(10 * total, 500)
+        assert st.units == total - 500
+        assert head + tail == golden["published"]["squares"]["6"]
+        assert plan.solve(1000, total - 3)[0] == plan.solve(3, total - 3)[0]
+    finally:
+        plan.close()
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_lunnon_ranges_tile_the_count(engine, cuda, golden, mode):
+    """Prefix-state ranges (gpu_folding_v2's max_states): a range past the
+    last state counts 0 and consecutive ranges sum to the whole map."""
+    plan = engine.LunnonPlan((4, 5))
+    states = plan.count_prefixes(10)
+    assert plan.count_range(10, states, 0, mode)[:2] == (0, 0)
+    parts = [plan.count_range(10, s, 37, mode) for s in range(0, states, 37)]
+    assert sum(p[1] for p in parts) == states
+    assert sum(p[0] for p in parts) == golden["lunnon"]["4x5"]
