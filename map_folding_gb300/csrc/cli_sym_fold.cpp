@@ -13,10 +13,13 @@
 // by default on 9x9), MF_SEED_START / MF_SEED_COUNT and its stderr lines
 // (sym_fold9.cpp:963-1198); counting past cell 63 uses the 128-bit kernel.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <thread>
 
@@ -52,6 +55,55 @@ bool parse_size(const char *text, unsigned long long &out) {
     out = std::strtoull(text, &end, 10);
     return *text != '\0' && *end == '\0';
 }
+
+// Cases selected for the device and cases whose count is back, for the
+// progress lines.
+struct Progress {
+    std::atomic<unsigned long long> selected{0}, completed{0};
+    std::atomic<int> producer_done{0};
+};
+
+// The reference's progress thread (sym_fold.cpp:442-454 materialized,
+// :574-589 streaming): a line every 5 s while the count runs, none after.
+class ProgressPrinter {
+  public:
+    ProgressPrinter(const Progress &p, bool stream, unsigned long long planned)
+        : p_(p), stream_(stream), planned_(planned), start_(Clock::now()), thread_([this] { run(); }) {}
+    ~ProgressPrinter() {
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            done_ = true;
+        }
+        cv_.notify_all();
+        thread_.join();
+    }
+
+  private:
+    void run() {
+        std::unique_lock<std::mutex> lock(mu_);
+        while (!done_) {
+            if (cv_.wait_for(lock, std::chrono::seconds(5), [this] { return done_; })) break;
+            const unsigned long long c = p_.completed.load();
+            const double el = since(start_);
+            const double rate = el > 0.0 ? double(c) / el : 0.0;
+            if (stream_)
+                std::fprintf(stderr,
+                             "stream selected=%llu completed=%llu producer_done=%d rate=%g/s elapsed_s=%g\n",
+                             p_.selected.load(), c, p_.producer_done.load(), rate, el);
+            else
+                std::fprintf(stderr, "progress=%llu/%llu rate=%g/s elapsed_s=%g\n", c, planned_, rate, el);
+        }
+    }
+
+    const Progress &p_;
+    const bool stream_;
+    const unsigned long long planned_;
+    const Clock::time_point start_;
+    std::mutex mu_;
+    std::condition_variable cv_;
+    bool done_ = false;
+    std::thread thread_;  // last: starts once the members above exist
+};
 
 void usage(const char *exe) {
     std::fprintf(stderr, "Usage: %s n [threads] [max_cases] [start_case]\nExample: %s 6 12\n", exe,
@@ -259,7 +311,42 @@ int main(int argc, char **argv) {
                 }
             }
         }
-        const int rc = mf_sym_plan_solve(plan, max_cases, start_case, mode, nullptr, answer, &st);
+        // The chunk runs as consecutive pieces so that finished cases can be
+        // reported: the first piece is at most 4096 cases, later ones are
+        // sized from the measured rate to take about 5 s.  Counts add up
+        // exactly (the answer is linear in the cases).
+        unsigned long long planned = total > start_case ? total - start_case : 0;
+        if (max_cases && max_cases < planned) planned = max_cases;
+        int rc = MF_OK;
+        {
+            Progress prog;
+            ProgressPrinter printer(prog, stream, planned);
+            unsigned __int128 sum = 0;
+            unsigned long long done = 0;
+            unsigned long long piece = std::min<unsigned long long>(planned, 4096);
+            while (done < planned) {
+                prog.selected = done + piece;
+                if (done + piece == planned) prog.producer_done = 1;
+                const auto ts = Clock::now();
+                uint64_t part[2] = {0, 0};
+                mf_run_stats ps{};
+                rc = mf_sym_plan_solve(plan, piece, start_case + done, mode, nullptr, part, &ps);
+                if (rc != MF_OK) break;
+                sum += (static_cast<unsigned __int128>(part[1]) << 64) | part[0];
+                st.kernel_s += ps.kernel_s;
+                st.units += ps.units;
+                st.nodes += ps.nodes;
+                st.splits += ps.splits;
+                done += piece;
+                prog.completed = done;
+                const double el = since(ts);
+                const double rate = el > 0.0 ? double(piece) / el : 1e9;
+                const double next = std::max(4096.0, std::min(5.0 * rate, 1e15));
+                piece = std::min<unsigned long long>(planned - done, (unsigned long long)next);
+            }
+            answer[0] = uint64_t(sum);
+            answer[1] = uint64_t(sum >> 64);
+        }
         mf_sym_plan_destroy(plan);
         if (rc != MF_OK) {
             std::fprintf(stderr, "error: %s\n", mf_last_error());

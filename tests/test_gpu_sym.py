@@ -174,6 +174,24 @@ def test_sym_fold_cli_stream_chunk(engine, cuda, golden):
     assert "n=8 threads=16 max_cases=200 start_case=0 total_s=" in r.stderr
 
 
+def test_sym_fold_cli_progress_lines_7x7(engine, cuda, golden):
+    """The whole 7x7 through the CLI: the answer (the chunk runs as pieces
+    whose counts add up), and the reference's `progress=c/total rate=
+    elapsed_s=` lines every 5 s while it runs (sym_fold.cpp:442-454)."""
+    import re
+
+    r = _cli("sym_fold", 7, 4)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip() == str(golden["published"]["squares"]["7"])
+    lines = re.findall(r"^progress=(\d+)/(\d+) rate=[0-9.e+-]+/s elapsed_s=([0-9.e+-]+)$",
+                       r.stderr, re.M)
+    assert len(lines) >= 3, r.stderr  # two or more ticks, then the final line
+    done = [int(c) for c, _, _ in lines]
+    assert all(t == "433131" for _, t, _ in lines)
+    assert done == sorted(done) and done[-1] == 433131
+    assert float(lines[0][2]) >= 4.5
+
+
 def test_sym_fold_cli_full_6(engine, cuda, golden):
     for mode in ("plain", "batched"):
         r = _cli("sym_fold", 6, 4, env={"MF_GPU_MODE": mode})
