@@ -6,7 +6,9 @@
 // key=value lines as sym_fold.cpp:622-774, including MF_STREAM_CASES,
 // MF_EXPANDED_N and MF_SETUP_ONLY.  The counting runs on the GPU; `threads`
 // is accepted and echoed.  MF_GPU_MODE=plain selects the one-thread-per-case
-// kernel instead of the batched work-stealing one.
+// kernel instead of the batched work-stealing one.  A long chunk runs as
+// consecutive pieces of about 5 s, so that a progress thread can print the
+// reference's progress lines with exact finished-case counts.
 //
 // Built with -DMF_SYM_FOLD9 this is the drop-in for
 // experiments/9x9/sym_fold9.cpp instead: n up to 9, MF_CENTER_N (5x5 centre
