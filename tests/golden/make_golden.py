@@ -6,6 +6,7 @@ solvers, built from source by `make -C oracle ref` into oracle/_ref/.
     python tests/golden/make_golden.py --sym9   # refresh only the sym_fold9 (9x9) vectors
     python tests/golden/make_golden.py --high-dim  # refresh only the 3- to 5-D Lunnon maps
     python tests/golden/make_golden.py --published # rewrite only the published values
+    python tests/golden/make_golden.py --serving   # the serving stream's 8x8 chunks (hours, resumable)
 
 Every value in the output was printed by an unmodified reference binary on
 this machine; published values quoted in the reference's documents are kept
@@ -224,6 +225,38 @@ PUBLISHED = {
 }
 
 
+def serving_chunks(seed=5, requests=12, rate=0.15):
+    """The 8x8 chunk requests of the serving benchmark's default stream:
+    50,000 consecutive depth-36 cases from seeded uniform starts."""
+    sys.path.insert(0, str(ROOT))
+    from map_folding_gb300.workloads import serving_stream
+
+    return [(r.start_case, r.max_cases) for r in serving_stream(seed, requests, rate)
+            if r.kind == "chunk"]
+
+
+def main_serving():
+    """Count every 8x8 chunk of the serving stream with the reference's own
+    sym_fold (MF_STREAM_CASES=1 MF_EXPANDED_N=36, all host threads).  Each
+    chunk takes minutes to an hour of CPU, so results are written into
+    reference_counts.json["sym_serving"] one chunk at a time and chunks that
+    are already there are skipped: the run can be stopped and resumed."""
+    path = HERE / "reference_counts.json"
+    threads = str(os.cpu_count())
+    for start, cases in serving_chunks():
+        key = f"8x8_d36_{start}+{cases}"
+        out = json.loads(path.read_text())
+        if key in out.get("sym_serving", {}):
+            continue
+        count = run([REF / "sym_fold", 8, threads, cases, start],
+                    {"MF_STREAM_CASES": "1", "MF_EXPANDED_N": "36"})
+        out = json.loads(path.read_text())
+        out.setdefault("sym_serving", {})[key] = {"count": int(count), "start_case": start,
+                                                  "max_cases": cases, "expanded_n": 36}
+        path.write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
+        print(key, count, flush=True)
+
+
 def main_published():
     """Rewrite only the published section (values quoted from the reference's documents)."""
     path = HERE / "reference_counts.json"
@@ -272,5 +305,7 @@ if __name__ == "__main__":
         main_high_dim()
     elif "--published" in sys.argv:
         main_published()
+    elif "--serving" in sys.argv:
+        main_serving()
     else:
         main()
