@@ -196,6 +196,23 @@ int32_t mf_sym_count_cases(int32_t n, int32_t start_i, int32_t stop_i,
                            const uint8_t *d_cycles, uint64_t num_cases,
                            uint64_t *d_counts, uint64_t *d_nodes, void *stream);
 
+/* Header of a persistent (batched) launch, the first 64 bytes of its
+ * workspace. */
+typedef struct {
+    uint64_t units_handed_out; /* initial units claimed (may exceed the count) */
+    uint64_t split_head;       /* split items taken */
+    uint64_t split_items;      /* split items created by device-side splitting */
+    uint64_t completed;        /* units + split items finished */
+    uint64_t work_items_run;
+    uint32_t error;            /* 0, MF_RUN_MALFORMED or MF_RUN_WAIT_LIMIT */
+    uint32_t pad;
+    int64_t idle_lanes;
+    uint64_t warps_out;        /* warps that have left the launch */
+} mf_run_header;
+
+#define MF_RUN_MALFORMED 1u  /* a unit's list was not a permutation */
+#define MF_RUN_WAIT_LIMIT 2u /* the launch ended with work unaccounted for */
+
 /* Device workspace the batched sym kernel needs for `cfg`. */
 uint64_t mf_sym_workspace_bytes(const mf_batch_config *cfg);
 
@@ -204,9 +221,15 @@ uint64_t mf_sym_workspace_bytes(const mf_batch_config *cfg);
  * mf_sym_count_cases.  d_workspace (256-byte aligned) must hold
  * mf_sym_workspace_bytes(cfg) bytes.  The launch is asynchronous on
  * `stream`; once it has completed, the workspace's first 64 bytes hold the
- * run's header: uint64 split items at byte 16, uint64 work items run at
- * byte 32, uint32 error flag at byte 40 (non-zero: a malformed case was
- * seen and the kernel stopped early, the counts are not valid).
+ * run's header (mf_run_header above).  The counts are valid only if its
+ * error word is 0 and completed == num_cases + split_items.  Error word 1
+ * (MF_RUN_MALFORMED): a case's cycle is not a permutation of its placed
+ * cells; that case's count is UINT64_MAX and the kernel stopped early.
+ * Error word 2 (MF_RUN_WAIT_LIMIT): the launch ended with work still
+ * unaccounted for.  Every device-side wait is bounded: an idle warp leaves
+ * after cfg->wait_limit idle rounds (normal while other warps finish the
+ * work), and the last warp out raises this word if the work accounting has
+ * not closed -- a split item that was never published, say.
  * Replaces: the same reference lines as mf_sym_count_cases; the reference
  * balances only across host threads (sym_fold.cpp:456-488). */
 int32_t mf_sym_count_cases_batched(int32_t n, int32_t start_i, int32_t stop_i,
@@ -263,19 +286,32 @@ int32_t mf_sym_sort_order(const uint64_t *scores, const uint64_t *mults, uint64_
  * device synchronisation of cudaMalloc/cudaFree.  The split-item ring lives
  * in a fixed __device__ array of 4096 cells (416.25 KiB, plus 2.25 KiB of
  * edge pages) that every GPU loading this library holds until the process
- * exits; a cfg->queue_capacity above 4096 is rejected with MF_ERR_CAPACITY.
+ * exits.  The ring always has those 4096 cells: a cfg->queue_capacity above
+ * 4096 is rejected with MF_ERR_CAPACITY, a smaller one is ignored, and
+ * cfg->stack_mode 2 (the 128-bit kernel) is rejected with MF_ERR_ARG.
  * The caller still passes inputs and outputs (d_cycles, d_counts, d_nodes).
- * The first call on a device performs its one-time set-up (looks up the
- * array's device address and copies the edge pages in), so make that first
- * call before any stream capture.  All calls share the array and it keeps the
- * last call's contents; each call clears what must start at zero, but calls
- * that overlap on the GPU (concurrent streams, other host threads) race on it
- * and must be serialised by the caller.  It calls no cudaMalloc, cudaFree or
- * other allocating routine. */
+ * The first call on a device (and the first after a device reset) performs
+ * its one-time set-up (looks up the array's device address and copies the
+ * edge pages in), so make that first call before any stream capture.  All
+ * calls share the array and it keeps the last call's contents; each call
+ * clears what must start at zero, but calls that overlap on the GPU
+ * (concurrent streams, other host threads) race on it and must be
+ * serialised by the caller.  The run's header, with its error word, stays in
+ * the array: read it with mf_sym_static_status after the launch (a malformed
+ * case also reads UINT64_MAX in d_counts).  It calls no cudaMalloc, cudaFree
+ * or other allocating routine. */
 int32_t mf_sym_count_cases_batched_static(int32_t n, int32_t start_i, int32_t stop_i,
                                           const uint8_t *d_cycles, uint64_t num_cases,
                                           uint64_t *d_counts, uint64_t *d_nodes,
                                           const mf_batch_config *cfg, void *stream);
+
+/* Copies the header of the last mf_sym_count_cases_batched_static run on
+ * the current device (an mf_run_header, 64 bytes) into dst -- host or
+ * device memory -- asynchronously on `stream`, after the work queued there
+ * before it.  The run's counts are valid only if its error word is 0 and
+ * completed == num_cases + split_items.  Allocates nothing.
+ * No counterpart in the reference. */
+int32_t mf_sym_static_status(void *stream, void *dst);
 
 /* ---- CUDA-graph replay ------------------------------------------------ */
 
@@ -377,6 +413,22 @@ int32_t mf_sym_solve(int32_t n, uint64_t max_cases, uint64_t start_case, int32_t
 uint32_t mf_solve_cases(uint32_t n, uint32_t start_i, uint32_t stop_i,
                         const uint8_t *case_buffer, uint32_t case_count,
                         uint32_t *output_words);
+
+/* ======================================================================
+ * Test support
+ * ====================================================================== */
+
+/* Host-side fault injection for tests of the bounded device waits.  With
+ * MF_FAULT_LOST_SPLIT the next persistent launch (batched sym or Lunnon,
+ * 64-bit) starts with one split-ring ticket reserved that no lane will ever
+ * publish -- a donor's message lost on the way -- so the split items behind
+ * it are never taken, the work accounting cannot close, the idle warps
+ * leave after cfg->wait_limit rounds and the last one out raises error word
+ * MF_RUN_WAIT_LIMIT (the host-buffer entry points then return
+ * MF_ERR_TIMEOUT).  Nothing on the device faults or hangs.  One-shot; 0
+ * clears it.  No counterpart in the reference. */
+#define MF_FAULT_LOST_SPLIT 1u
+void mf_test_inject_fault(uint32_t kind);
 
 #ifdef __cplusplus
 }

@@ -88,6 +88,26 @@ class RequestInfo(ctypes.Structure):
     ]
 
 
+class RunHeader(ctypes.Structure):
+    """mf_run_header: the 64-byte header of a persistent launch."""
+    _fields_ = [
+        ("units_handed_out", ctypes.c_uint64),
+        ("split_head", ctypes.c_uint64),
+        ("split_items", ctypes.c_uint64),
+        ("completed", ctypes.c_uint64),
+        ("work_items_run", ctypes.c_uint64),
+        ("error", ctypes.c_uint32),
+        ("pad", ctypes.c_uint32),
+        ("idle_lanes", ctypes.c_int64),
+        ("warps_out", ctypes.c_uint64),
+    ]
+
+
+MF_RUN_MALFORMED = 1
+MF_RUN_WAIT_LIMIT = 2
+MF_FAULT_LOST_SPLIT = 1
+
+
 class EngineError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"mapfold status {status}: {message}")
@@ -121,6 +141,8 @@ SIGNATURES = {
     "mf_sym_sort_order": ([_p, _p, _u64, _i32, _p], _i32),
     "mf_sym_plan_block_costs": ([_p, _u64, _u64, _i32, _u64, _i32, _p, _p], _i32),
     "mf_sym_count_cases_batched_static": ([_i32, _i32, _i32, _p, _u64, _p, _p, _p, _p], _i32),
+    "mf_sym_static_status": ([_p, _p], _i32),
+    "mf_test_inject_fault": ([_u32], None),
     "mf_sym_graph_create": ([_i32, _i32, _i32, _p, _u64, _p, _p, _p, _u64, _p,
                              ctypes.POINTER(_p)], _i32),
     "mf_graph_launch": ([_p, _p], _i32),

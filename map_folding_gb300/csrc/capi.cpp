@@ -1,5 +1,6 @@
 // capi.cpp -- the extern "C" entry points declared in include/mapfold.h.
 #include <algorithm>
+#include <cstddef>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -36,6 +37,37 @@ BatchKnobs resolve_knobs(const mf_batch_config *cfg) {
     while (cap < k.queue_capacity && cap < (1ULL << 26)) cap <<= 1;
     k.queue_capacity = cap;
     return k;
+}
+
+static_assert(sizeof(QueueHeader) == sizeof(mf_run_header), "mf_run_header mirrors QueueHeader");
+static_assert(offsetof(QueueHeader, error) == offsetof(mf_run_header, error), "error word offset");
+static_assert(offsetof(QueueHeader, completed) == offsetof(mf_run_header, completed),
+              "completed offset");
+static_assert(kErrMalformed == MF_RUN_MALFORMED && kErrWaitLimit == MF_RUN_WAIT_LIMIT,
+              "error words");
+
+int check_queue_header(const QueueHeader &hdr, uint64_t units) {
+    if (hdr.error == kErrMalformed) {
+        set_error("a unit's list is not a permutation of its placed items (malformed input)");
+        return MF_ERR_ARG;
+    }
+    if (hdr.error == kErrWaitLimit) {
+        set_error("a bounded device-side wait ran out with work still unaccounted for");
+        return MF_ERR_TIMEOUT;
+    }
+    if (hdr.error) {
+        set_error("the persistent kernel reported error word %u", hdr.error);
+        return MF_ERR_TIMEOUT;
+    }
+    if (units && (hdr.init_next < units || hdr.completed != units + hdr.spawn_tail)) {
+        set_error("work accounting does not close: %llu of %llu units handed out, %llu items "
+                  "completed of %llu units + %llu split items",
+                  (unsigned long long)hdr.init_next, (unsigned long long)units,
+                  (unsigned long long)hdr.completed, (unsigned long long)units,
+                  (unsigned long long)hdr.spawn_tail);
+        return MF_ERR_TIMEOUT;
+    }
+    return MF_OK;
 }
 
 namespace {
@@ -432,10 +464,7 @@ static int32_t lunnon_batch_impl(const mf_lunnon_plan *const *plans, int32_t num
     cudaEventRecord(td.b, st);
     MF_TRY_CUDA(cudaStreamSynchronize(st));
     const QueueHeader *hdr = reinterpret_cast<const QueueHeader *>(h_counts + num_plans + 1);
-    if (hdr->error) {
-        set_error("batched kernel reported a device wait timeout or malformed state");
-        return MF_ERR_TIMEOUT;
-    }
+    if (int rc = check_queue_header(*hdr, total)) return rc;
     for (int k = 0; k < num_plans; ++k) counts_out[k] = h_counts[k];
     if (stats) {
         *stats = mf_run_stats{};
@@ -699,10 +728,7 @@ int32_t mf_lunnon_batch_run(mf_lunnon_batch *b, uint64_t *counts_out, mf_run_sta
     cudaEventRecord(td.b, b->stream);
     MF_TRY_CUDA(cudaStreamSynchronize(b->stream));
     const QueueHeader *hdr = reinterpret_cast<const QueueHeader *>(b->h_out + np + 1);
-    if (hdr->error) {
-        set_error("batched kernel saw a malformed prefix state");
-        return MF_ERR_TIMEOUT;
-    }
+    if (int rc = check_queue_header(*hdr, b->units)) return rc;
     for (int k = 0; k < np; ++k) counts_out[k] = b->h_out[k];
     if (stats) {
         *stats = mf_run_stats{};
@@ -936,10 +962,8 @@ int count_cases_host(int n, int start_i, int stop_i, const uint8_t *h_cycles, ui
     QueueHeader hdr{};
     if (mode == 1) std::memcpy(&hdr, h_hdr, sizeof(hdr));
     if (hdr_out) *hdr_out = hdr;
-    if (hdr.error) {
-        set_error("batched kernel reported a device wait timeout or malformed case");
-        return MF_ERR_TIMEOUT;
-    }
+    if (mode == 1)
+        if (int rc = check_queue_header(hdr, num)) return rc;
     for (uint64_t k = 0; k < num; ++k)
         if (h_counts[k] == ~0ULL) {
             set_error("case %llu is not a consistent cycle", (unsigned long long)k);

@@ -413,6 +413,24 @@ __device__ __forceinline__ int ring_claim(const Queue &Q, unsigned long long *co
     return __shfl_sync(kFull, got, 0);
 }
 
+// Called once per warp (lane 0) as it leaves a persistent launch, after all
+// of its counters are in.  Warps leave early on purpose (idle for wait_limit
+// rounds while others still work), so only the last warp out can tell
+// whether the launch ended with work unaccounted for -- every initial unit
+// handed out and completed == units + split items -- and, if not, raises
+// error word kErrWaitLimit: some bounded wait ran out before the work was
+// done (a split item that was never published, say).
+__device__ __forceinline__ void leave_and_check(QueueHeader *hdr, unsigned long long units) {
+    __threadfence();
+    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
+    const unsigned long long out = atomicAdd(&hdr->warps_out, 1ULL) + 1;
+    if (out != warps) return;
+    __threadfence();
+    const bool closed = vload(&hdr->init_next) >= units &&
+                        vload(&hdr->completed) == units + vload(&hdr->spawn_tail);
+    if (!closed) atomicCAS(&hdr->error, 0u, kErrWaitLimit);
+}
+
 // Copy ticket t's item out and free its cell for the producer of t + capacity.
 __device__ __forceinline__ void ring_take(const Queue &Q, unsigned long long t, uint32_t (&w)[24]) {
     const unsigned long long cell = t & (Q.capacity - 1);

@@ -23,6 +23,7 @@
 // (plain) or raises the queue error flag (batched).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -136,7 +137,8 @@ struct LunnonSource {
 // shallowest untried siblings.  A warp leaves when it is idle and all work is
 // accounted for, or when it has stayed idle for wait_limit rounds; leaving is
 // always safe, because the warp that owns a split item's parent keeps looping
-// until it has nothing left.
+// until it has nothing left.  The last warp out checks that the work
+// accounting closed (leave_and_check).
 template <int TPB, int WORDS, bool kSym, class Stk>
 __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
                                                 const LunnonInstanceDev *s_inst,
@@ -296,7 +298,11 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
                     ok = list_valid(L, root < lrules.n + 1 ? root : lrules.n + 1);
                 }
                 if (!ok) {
-                    atomicExch(&Q.hdr->error, 1u);
+                    atomicExch(&Q.hdr->error, kErrMalformed);
+                    // As the plain kernel does: the case's count slot says it
+                    // was not counted (a Lunnon slot is a whole map's sum and
+                    // keeps only the error word).
+                    if (kSym) counts[owner] = ~0ULL;
                     ++finished;
                 } else if (root > last) {  // nothing left to place: one completion
                     leaves = 1;
@@ -409,6 +415,7 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
     if (lane == 0) {
         if (nodes_out && ns) atomicAdd(nodes_out, ns);
         if (st) atomicAdd(&Q.hdr->tasks_run, st);
+        leave_and_check(Q.hdr, num);
     }
 }
 
@@ -549,10 +556,18 @@ Queue carve_queue(void *ws, uint64_t capacity) {
     return q;
 }
 
+// Host-side fault injection for tests (mf_test_inject_fault): the next
+// persistent launch starts with one split-ring ticket reserved that no lane
+// ever publishes, as if a donor's message had been lost.
+std::atomic<uint32_t> g_inject{0};
+
+__global__ void phantom_ticket_kernel(QueueHeader *hdr) { hdr->spawn_tail = 1; }
+
 cudaError_t reset_queue(const Queue &Q, cudaStream_t stream) {
     cudaError_t e = cudaMemsetAsync(Q.hdr, 0, 256, stream);
     if (e != cudaSuccess) return e;
     ring_init_kernel<<<64, 256, 0, stream>>>(Q.seq, Q.capacity);
+    if (g_inject.exchange(0) == MF_FAULT_LOST_SPLIT) phantom_ticket_kernel<<<1, 1, 0, stream>>>(Q.hdr);
     return cudaGetLastError();
 }
 
@@ -732,6 +747,7 @@ __device__ __align__(256) uint8_t g_static_edges[9][4 * kSymCells];  // edge pag
 
 struct StaticState {
     bool ready = false;
+    unsigned long long ctx_id = 0;  // the CUDA context the addresses belong to
     void *workspace = nullptr;
     uint8_t *edges = nullptr;
 };
@@ -739,25 +755,65 @@ struct StaticState {
 std::mutex g_static_mu;
 StaticState g_static[64];
 
-// Once per device, with that device current: look up the arrays' device
-// addresses (a host-side name of a __device__ array is not a device address)
-// and fill the edge pages of every board size.
+// Unique id of the calling thread's current CUDA context (0 if none can be
+// read).  A device reset destroys the primary context and reloads this
+// module with zeroed __device__ arrays; the next context gets a new id.
+unsigned long long current_context_id() {
+    using GetCurrent = int (*)(void **);
+    using GetId = int (*)(void *, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+    });
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// Once per device and context, with that device current: look up the
+// arrays' device addresses (a host-side name of a __device__ array is not a
+// device address) and fill the edge pages of every board size.  Done again
+// if the context changed since (a device reset), so no stale address or
+// zeroed edge page is ever used.
 int static_setup(int dev, StaticState *&out) {
     std::lock_guard<std::mutex> lock(g_static_mu);
     StaticState &s = g_static[dev];
-    if (!s.ready) {
-        void *ws = nullptr, *edges = nullptr;
-        MF_TRY_CUDA(cudaGetSymbolAddress(&ws, g_static_workspace));
+    void *ws = nullptr;
+    MF_TRY_CUDA(cudaGetSymbolAddress(&ws, g_static_workspace));  // also brings the context up
+    const unsigned long long ctx = current_context_id();
+    if (!s.ready || (ctx != 0 && ctx != s.ctx_id)) {
+        void *edges = nullptr;
         MF_TRY_CUDA(cudaGetSymbolAddress(&edges, g_static_edges));
         uint8_t host[9][4 * kSymCells] = {};
         for (int n = 2; n <= 8; ++n) sym_edges(n, host[n]);
         MF_TRY_CUDA(cudaMemcpy(edges, host, sizeof(host), cudaMemcpyHostToDevice));
         s.workspace = ws;
         s.edges = static_cast<uint8_t *>(edges);
+        s.ctx_id = ctx;
         s.ready = true;
     }
     out = &s;
     return MF_OK;
+}
+
+int current_static_state(StaticState *&s) {
+    int dev = 0;
+    MF_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_error("device ordinal %d out of range", dev);
+        return MF_ERR_ARG;
+    }
+    return static_setup(dev, s);
 }
 
 }  // namespace
@@ -794,15 +850,12 @@ extern "C" int32_t mf_sym_count_cases_batched_static(int32_t n, int32_t start_i,
         set_error("d_cycles must be 16-byte aligned");
         return MF_ERR_ARG;
     }
-    int dev = 0;
-    MF_TRY_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) {
-        set_error("device ordinal %d out of range", dev);
+    if (cfg && cfg->stack_mode == 2) {
+        set_error("stack_mode 2 (the 128-bit kernel) has no allocation-free form");
         return MF_ERR_ARG;
     }
     StaticState *s = nullptr;
-    int rc = static_setup(dev, s);
-    if (rc) return rc;
+    if (int rc = current_static_state(s)) return rc;
     BatchKnobs knobs = resolve_knobs(cfg);
     knobs.queue_capacity = kStaticRingCells;
     MF_TRY_CUDA(launch_sym_batched(s->edges + size_t(n) * 4 * kSymCells, start_i, stop_i, d_cycles,
@@ -810,3 +863,19 @@ extern "C" int32_t mf_sym_count_cases_batched_static(int32_t n, int32_t start_i,
                                    static_cast<cudaStream_t>(stream)));
     return MF_OK;
 }
+
+extern "C" int32_t mf_sym_static_status(void *stream, void *dst) {
+    using namespace mf;
+    clear_error();
+    if (!dst) {
+        set_error("dst is required");
+        return MF_ERR_ARG;
+    }
+    StaticState *s = nullptr;
+    if (int rc = current_static_state(s)) return rc;
+    MF_TRY_CUDA(cudaMemcpyAsync(dst, s->workspace, sizeof(QueueHeader), cudaMemcpyDefault,
+                                static_cast<cudaStream_t>(stream)));
+    return MF_OK;
+}
+
+extern "C" void mf_test_inject_fault(uint32_t kind) { mf::g_inject.store(kind); }

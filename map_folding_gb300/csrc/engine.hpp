@@ -154,12 +154,23 @@ struct QueueHeader {
     unsigned long long spawn_tail;  // split items reserved
     unsigned long long completed;   // work items finished
     unsigned long long tasks_run;
-    unsigned int error;             // 1: a malformed unit was seen
+    unsigned int error;             // 0, kErrMalformed or kErrWaitLimit
     unsigned int pad;
     long long idle_lanes;           // lanes waiting for work (warps report deltas)
-    long long reserved;
+    unsigned long long warps_out;   // warps that have left the launch
 };
 static_assert(sizeof(QueueHeader) == 64, "queue header layout");
+
+// Error words of a persistent launch (QueueHeader::error).
+constexpr unsigned int kErrMalformed = 1;  // a unit's list was not a permutation
+constexpr unsigned int kErrWaitLimit = 2;  // the launch ended (its warps' bounded
+                                           // waits ran out) with work unaccounted for
+
+// After a persistent launch: MF_OK, or the status its header reports --
+// MF_ERR_ARG for a malformed unit, MF_ERR_TIMEOUT when a bounded wait ran
+// out or the work accounting does not close (every initial unit handed out,
+// completed == units + split items).  Sets the error text.
+int check_queue_header(const QueueHeader &hdr, uint64_t units);
 
 uint64_t workspace_bytes(uint64_t capacity);
 uint64_t wide_workspace_bytes(uint64_t capacity);

@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
     SymRules srules = sym_rules(smem);
     LunnonRules lrules{A.tables, 0, 0};
     unsigned long long leaves = 0, nodes = 0, unit_nodes0 = 0;
-    uint32_t idle_rounds = 0, round = 0, nap = 256;
+    uint32_t idle_rounds = 0, stuck_rounds = 0, round = 0, nap = 256;
     int reported_idle = 0;
     bool ring_hint = false;
 
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
                 unit_nodes0 = nodes;
                 const int placed = kind == 0 ? root : (root < lrules.n + 1 ? root : lrules.n + 1);
                 if (!list_valid(L, placed)) {
-                    atomicExch(&A.ctl->error, 1u);
+                    atomicExch(&A.ctl->error, kErrMalformed);
                     finish();
                 } else if (root > last) {
                     leaves = 1;
@@ -269,7 +269,17 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
                                   vload(&A.Q.hdr->spawn_tail) != vload(&A.Q.hdr->spawn_head);
                 stop = !work && (*reinterpret_cast<volatile unsigned int *>(&A.ctl->stop) != 0u ||
                                  ++idle_rounds > A.wait_limit);
-                if (work) idle_rounds = 0;
+                if (work) {
+                    idle_rounds = 0;
+                    // Work is pending but this idle warp got none of it this
+                    // round.  A published unit or split item is claimable at
+                    // once, so wait_limit such rounds in a row mean an item
+                    // that is never published: report it and leave.
+                    if (++stuck_rounds > A.wait_limit) {
+                        atomicCAS(&A.ctl->error, 0u, kErrWaitLimit);
+                        stop = 1;
+                    }
+                }
             }
             stop = __shfl_sync(kFull, stop, 0);
             if (stop) break;
@@ -279,6 +289,7 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
             continue;
         }
         nap = 256;
+        stuck_rounds = 0;
         if (busy) {
             const uint64_t g = evaluate();
             eval = apply_advance(L, S, lvl, eval, root, last, fresh, g, leaves);
@@ -660,8 +671,19 @@ void pump_loop(mf_server *s) {
         publish_oldest(s);
         // Keep the kernel alive while work is resident.
         if (s->running > 0) {
-            if (s->kernel_live && cudaStreamQuery(s->kstream) == cudaSuccess) s->kernel_live = false;
-            if (!s->kernel_live) {
+            if (s->kernel_live && cudaStreamQuery(s->kstream) == cudaSuccess) {
+                s->kernel_live = false;
+                // A kernel that left with requests still running either ran
+                // out of work to wait for (relaunch it) or reported an error.
+                unsigned int err = 0;
+                if (cudaMemcpy(&err, &s->d_ctl->error, sizeof(err), cudaMemcpyDeviceToHost) != cudaSuccess)
+                    s->failure = "reading the server kernel's error word failed";
+                else if (err == kErrWaitLimit)
+                    s->failure = "the server kernel gave up waiting for a split item that was never published";
+                else if (err)
+                    s->failure = "the server kernel saw a malformed unit";
+            }
+            if (!s->kernel_live && s->failure.empty()) {
                 const unsigned int zero = 0;
                 cudaMemcpy(&s->d_ctl->stop, &zero, sizeof(zero), cudaMemcpyHostToDevice);
                 if (launch_server_kernel(s) == cudaSuccess) s->kernel_live = true;

@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(TPB)
                     root = start_i;
                     ++started;
                     if (!list_valid(L, start_i)) {
-                        atomicExch(&Q.hdr->error, 1u);
+                        atomicExch(&Q.hdr->error, kErrMalformed);
                         ++finished;
                     } else if (start_i > last) {
                         leaves = 1;
@@ -448,6 +448,7 @@ __global__ void __launch_bounds__(TPB)
     if (lane == 0) {
         if (nodes_out && ns) atomicAdd(nodes_out, ns);
         if (st) atomicAdd(&Q.hdr->tasks_run, st);
+        leave_and_check(Q.hdr, num);
     }
 }
 

@@ -14,11 +14,15 @@ from __future__ import annotations
 
 import ast
 import json
+import os
 import tempfile
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REFERENCE = Path("/root/reference")
+# The reference checkout: $MF_REFERENCE_DIR, else `reference` beside this
+# repository's checkout.
+REFERENCE = Path(os.environ.get("MF_REFERENCE_DIR")
+                 or Path(__file__).resolve().parents[3] / "reference")
 
 
 def reference_functions():

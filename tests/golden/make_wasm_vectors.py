@@ -8,11 +8,15 @@ from __future__ import annotations
 
 import base64
 import json
+import os
 import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REFERENCE = Path("/root/reference")
+# The reference checkout: $MF_REFERENCE_DIR, else `reference` beside this
+# repository's checkout.
+REFERENCE = Path(os.environ.get("MF_REFERENCE_DIR")
+                 or Path(__file__).resolve().parents[3] / "reference")
 
 # mfah/wasm/test_wasm.mjs:61-65
 TRIPLES = [(5, 14, 20, 16), (6, 14, 20, 16), (7, 14, 28, 64)]

@@ -47,6 +47,39 @@ def test_chunks_match_reference(engine, cuda, golden, key, n, e, count, start, m
     assert engine.sym_fold(n, count, start, expanded_n=e, mode=mode) == golden["sym"][key]
 
 
+# The reference's published 8x8 partial sums (EXPERIMENTS.md:77-81, kept in
+# reference_counts.json["published"]): each is what `sym_fold 8 ...` printed
+# for that chunk with MF_EXPANDED_N set.  The depth-36 100,000-case chunk is
+# twice the serving benchmark's chunk size.
+PUBLISHED_8X8 = [
+    # (published key, expanded_n, max_cases, start_case)
+    ("d36_first100000", 36, 100000, 0),
+    ("d32_first1000", 32, 1000, 0),
+    ("d24_case100000", 24, 1, 100000),
+    ("d24_case400000", 24, 1, 400000),
+]
+
+
+@pytest.mark.parametrize("key,e,count,start", PUBLISHED_8X8)
+def test_published_8x8_partial_sums(engine, cuda, golden, key, e, count, start):
+    want = golden["published"]["sym_8x8_partial_sums"][key]
+    assert engine.sym_fold(8, count, start, expanded_n=e, mode="batched") == want
+
+
+SERVING_GOLDEN = json.loads((ROOT / "tests" / "golden" / "reference_counts.json").read_text()
+                            ).get("sym_serving", {})
+
+
+@pytest.mark.parametrize("key", sorted(SERVING_GOLDEN))
+def test_serving_chunks_match_reference(engine, cuda, golden, key):
+    """The serving benchmark's 50,000-case 8x8 chunks (serving_stream(seed=5)),
+    against the reference's own sym_fold on the same chunk."""
+    rec = golden["sym_serving"][key]
+    got = engine.sym_fold(8, rec["max_cases"], rec["start_case"], expanded_n=rec["expanded_n"],
+                          mode="batched")
+    assert got == rec["count"]
+
+
 def _device_counts(engine, torch, n, start_i, stop_i, cycles, mode):
     d_cyc = torch.from_numpy(np.ascontiguousarray(cycles)).cuda()
     counts = torch.zeros(len(cycles), dtype=torch.int64, device="cuda")
