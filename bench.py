@@ -7,6 +7,10 @@ completion, i.e. the whole 7x7 answer 129950723279272, with the batched
 persistent work-stealing kernel.  Inputs are resident in HBM for `value`;
 `e2e` runs the same count through the C ABI with host buffers (case
 selection, host->device copy, kernel, device->host copy of per-case counts).
+After the timed steps, on one GPU: the plain one-thread-per-case kernel
+counts the same cases once (`batched_vs_plain`), and the serving stream's
+8x8 chunks run through the request server (`serving`: chunk p50/p99, each
+chunk checked against the reference's count).
 
 Metric: reference DFS nodes per second -- recurse_count calls of
 sym_fold.cpp:219, counted exactly by the kernel (and equal to the oracle's
@@ -41,6 +45,15 @@ UNIT = "nodes/s"
 # of the first 20,000 7x7 cases (2,106,880 + 1,431,552 bytes), per case.
 TRAFFIC_PER_CASE = (2_106_880 + 1_431_552) / 20_000
 
+# Issue profile of the batched kernel from the same ncu capture (first 20,000
+# 7x7 cases searched to completion, profiles/sym_batched_7x7_first20k.md):
+# warp instructions executed per reference node and active lanes per warp
+# instruction.  The bench scales the first by its own live node rate to get
+# the kernel's warp-instruction issue rate against the SMs' issue ceiling.
+ISSUE_PROFILE = {"warp_inst_per_node": 6.65e11 / 20_803_439_733, "lanes_per_inst": 12.15,
+                 "issue_active": 0.724, "alu_pipe": 0.625,
+                 "source": "profiles/sym_batched_7x7_first20k.md"}
+
 
 def work_counts() -> dict:
     """The whole 7x7 count's reference nodes and chain steps, counted by the
@@ -66,6 +79,38 @@ def issue_figures(nodes_per_step: int, t_step: float, clock_summary: dict) -> di
         if mhz:
             out["chain_steps_per_issue_slot"] = steps_s / (sms * 4 * mhz * 1e6)
     return out
+
+
+def issue_roofline(cases: int, nodes_per_step: int, t_step: float, clock_summary: dict) -> dict:
+    """The batched DFS kernel is bound by instruction issue, not by memory
+    (HBM carries only the 72-byte case records): achieved = warp instructions
+    per second (the ncu-measured warp instructions per node times the live
+    node rate), peak = one warp instruction per SMSP per cycle at the sampled
+    SM clock.  `useful_lane_frac` discounts inactive lanes.  The HBM figures
+    of the case loads are kept as a sub-record."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = clock_summary.get("sm_mhz") or clock_summary.get("sm_max_mhz") or 2070.0
+    peak = sms * 4 * mhz * 1e6 / 1e9
+    achieved = ISSUE_PROFILE["warp_inst_per_node"] * nodes_per_step / t_step / 1e9
+    algo_bytes = cases * (64 + 8)
+    hbm_peak, peak_kind = peaks()
+    hbm_achieved = algo_bytes / t_step / 1e9
+    return {
+        "bound": "int-issue", "achieved": achieved, "peak": peak, "unit": "Gwarp-inst/s",
+        "frac": achieved / peak, "peak_source": f"{sms} SMs x 4 SMSPs x 1 inst/clk at {mhz:.0f} MHz",
+        "lanes_per_inst": ISSUE_PROFILE["lanes_per_inst"],
+        "useful_lane_frac": achieved / peak * ISSUE_PROFILE["lanes_per_inst"] / 32,
+        "profile": ISSUE_PROFILE,
+        # ncu DRAM read + write of the first-20,000-case launch scaled by the
+        # case count
+        "traffic": TRAFFIC_PER_CASE * cases, "traffic_unit": "bytes per launch",
+        "hbm": {"achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": hbm_achieved / hbm_peak, "peak_source": peak_kind,
+                "algorithmic_bytes": algo_bytes},
+        "issue": issue_figures(nodes_per_step, t_step, clock_summary),
+    }
 
 
 def peaks():
@@ -135,19 +180,30 @@ def all_cases_7x7():
     return cyc, mult
 
 
+def strided_sample(cases, mults, count):
+    """`count` cases spread evenly over the whole case list (node cost varies
+    along the emission order, so a prefix would not represent the count)."""
+    import numpy as np
+
+    idx = np.unique(np.linspace(0, len(cases) - 1, count).round().astype(np.int64))
+    return np.ascontiguousarray(cases[idx]), np.ascontiguousarray(mults[idx])
+
+
 def time_cpu(cases, mults, threads, target_s=12.0):
     """Time the oracle (a restatement of sym_fold.cpp's solver) on growing
-    prefixes of the case list until one run takes ~target_s; returns
-    (nodes/s, sample description, seconds)."""
+    strided samples of the case list until one run takes ~target_s; returns
+    (nodes/s, sample description, seconds, sample size)."""
     from oracle import oracle
 
     count = 256
     while True:
+        c, m = strided_sample(cases, mults, count)
         t0 = time.perf_counter()
-        _, _, w = oracle.sym_count_cases(N, EXPANDED_N, cases[:count], mults[:count], threads)
+        _, _, w = oracle.sym_count_cases(N, EXPANDED_N, c, m, threads)
         el = time.perf_counter() - t0
         if el >= target_s * 0.5 or count >= len(cases):
-            return w.nodes / el, f"first {count} of {len(cases)} 7x7 depth-24 cases", el, count
+            return (w.nodes / el, f"{len(c)} cases evenly strided over all {len(cases)} 7x7 "
+                    f"depth-24 cases", el, count)
         count = min(len(cases), int(count * max(2.0, target_s / max(el, 1e-3))))
 
 
@@ -163,13 +219,14 @@ def run_reference(args):
     rate, sample, el, count = time_cpu(cases, mults, threads, target_s=8.0)
     from oracle import oracle
 
+    c, m = strided_sample(cases, mults, count)
     for _ in range(args.warmup):
-        oracle.sym_count_cases(N, EXPANDED_N, cases[:count], mults[:count], threads)
+        oracle.sym_count_cases(N, EXPANDED_N, c, m, threads)
     times = []
     nodes = 0
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        _, _, w = oracle.sym_count_cases(N, EXPANDED_N, cases[:count], mults[:count], threads)
+        _, _, w = oracle.sym_count_cases(N, EXPANDED_N, c, m, threads)
         times.append(time.perf_counter() - t0)
         nodes = w.nodes
     value = nodes * len(times) / sum(times)
@@ -259,10 +316,11 @@ def run_ours(args):
         dist.barrier()
     value = world * nodes_per_step * len(times) / float(t_max.item())
 
-    # End to end through the C ABI with host buffers.
+    # End to end through the C ABI with host buffers (a few repeats: every
+    # repeat is a whole 7x7 count).
     e2e_times = []
     e2e_st = None
-    for _ in range(args.steps):
+    for _ in range(max(1, min(args.steps, args.e2e_steps))):
         t0 = time.perf_counter()
         ans, st = plan.solve(0, 0, "batched")
         e2e_times.append(time.perf_counter() - t0)
@@ -270,9 +328,10 @@ def run_ours(args):
         e2e_st = st
     e2e_value = world * nodes_per_step * len(e2e_times) / sum(e2e_times)
 
-    # The plain one-thread-per-case kernel on the same cases, once.
+    # The plain one-thread-per-case kernel on the same cases, once (single
+    # GPU only: its ~430 s would hold the other ranks at the final barrier).
     plain_s = None
-    if args.plain:
+    if args.plain and world == 1:
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
@@ -283,20 +342,14 @@ def run_ours(args):
         plain_s = a.elapsed_time(b) * 1e-3
         assert check() == ANSWER_7X7
 
-    # Roofline: state-load bytes per launch (cases in, counts out) over the
-    # launch time, against measured HBM copy bandwidth.
-    algo_bytes = len(cycles) * (64 + 8)
-    hbm_peak, peak_kind = peaks()
-    achieved = algo_bytes / t_step / 1e9
     clock_summary = clocks.summary()
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak,
-                # ncu DRAM read + write of the first-20,000-case launch (3.54 MB,
-                # profiles/sym_batched_7x7_first20k.md) scaled by the case count
-                "traffic": TRAFFIC_PER_CASE * len(cycles), "traffic_unit": "bytes per launch",
-                "peak_source": peak_kind,
-                "note": "integer-issue/latency-bound DFS; HBM carries only the case loads",
-                "issue": issue_figures(nodes_per_step, t_step, clock_summary)}
+    roofline = issue_roofline(len(cycles), nodes_per_step, t_step, clock_summary)
+
+    # Config 5 in brief: the serving stream's 8x8 chunks through the resident
+    # server, every chunk checked against the reference's own count.
+    serving = None
+    if args.serving and world == 1:
+        serving = serving_summary(run_serving_stream(args.seed, args.requests, args.rate))
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -326,6 +379,7 @@ def run_ours(args):
             "plain_ms_per_step": None if plain_s is None else 1e3 * plain_s,
             "batched_vs_plain": None if plain_s is None else plain_s / t_step,
             "splits_per_step": int(e2e_st.splits) if e2e_st else None,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -473,26 +527,63 @@ def run_uneven(args, seed: int = 2026):
     print(json.dumps(line), flush=True)
 
 
-def run_serving(args):
-    """Config 5: 8x8 chunk requests (MF_EXPANDED_N=36, 50,000 consecutive
-    cases from a seeded uniform start) arriving as a Poisson stream,
-    interleaved with whole maps up to 5x6, through one resident server.
-    Latency is submit -> result; every chunk is recounted alone afterwards
-    (which also gives the alone capacity) and every map checked against the
-    reference's counts."""
-    import map_folding_gb300 as mf
+def run_serving_stream(seed: int, requests: int, rate: float) -> dict:
+    """The serving stream through one resident server: every chunk checked
+    against the reference's own sym_fold count of the same chunk (golden,
+    where tests/golden/make_golden.py --serving has made it) and every map
+    against the reference's count."""
     from map_folding_gb300.serving import Server, run_stream
     from map_folding_gb300.workloads import serving_stream
 
-    reqs = serving_stream(seed=args.seed, requests=args.requests, rate_per_s=args.rate,
-                          chunk_cases=50_000)
+    reqs = serving_stream(seed=seed, requests=requests, rate_per_s=rate, chunk_cases=50_000)
     golden = _golden_lunnon()
+    served = json.loads((ROOT / "tests" / "golden" / "reference_counts.json").read_text()
+                        ).get("sym_serving", {})
     with Server() as srv:
         # warm-up: the 8x8 expansion index and one small request of each kind
         srv.wait(srv.submit_sym(8, 36, 0, 100))
         srv.wait(srv.submit_lunnon((3, 4)))
         with ClockSampler(0) as clocks:
             out = run_stream(srv, reqs)
+    for r, q in zip(out["results"], reqs):
+        r["arrival_s"] = q.arrival_s
+        if r["kind"] == "chunk":
+            rec = served.get(f"8x8_d36_{r['start_case']}+{r['max_cases']}")
+            r["golden"] = rec is not None
+            if rec is not None:
+                assert r["answer"] == rec["count"], ("chunk differs from the reference", r["rid"])
+        else:
+            key = "x".join(map(str, sorted(r["dims"])))  # p x q and q x p fold alike
+            assert r["answer"] == golden[key], (key, r["answer"])
+            r["golden"] = True
+    out["clocks"] = clocks.summary()
+    out["seed"], out["rate_per_s"] = seed, rate
+    return out
+
+
+def serving_summary(out: dict) -> dict:
+    chunks = [r for r in out["results"] if r["kind"] == "chunk"]
+    return {"workload": "serving_stream: 8x8 MF_EXPANDED_N=36 50,000-case chunks + maps <= 5x6",
+            "seed": out["seed"], "requests": out["requests"], "rate_per_s": out["rate_per_s"],
+            "chunks": len(chunks), "chunks_golden": sum(r["golden"] for r in chunks),
+            "chunk_p50_s": out["chunk_p50_s"], "chunk_p99_s": out["chunk_p99_s"],
+            "all_p50_s": out["all_p50_s"], "all_p99_s": out["all_p99_s"],
+            "cases_per_s": out["cases_per_s"], "nodes_per_s": out["nodes_per_s"],
+            "wall_s": out["wall_s"], "clocks": out["clocks"],
+            "note": (f"p99 over {len(chunks)} chunks is their maximum" if len(chunks) < 100
+                     else "")}
+
+
+def run_serving(args):
+    """Config 5: 8x8 chunk requests (MF_EXPANDED_N=36, 50,000 consecutive
+    cases from a seeded uniform start) arriving as a Poisson stream,
+    interleaved with whole maps up to 5x6, through one resident server.
+    Latency is submit -> result; every chunk is checked against the
+    reference's count (golden) and recounted alone afterwards (which also
+    gives the alone capacity), every map against the reference's count."""
+    import map_folding_gb300 as mf
+
+    out = run_serving_stream(args.seed, args.requests, args.rate)
     plan = mf.SymPlan(8, 36)
     alone_s = 0.0
     cases = 0
@@ -503,27 +594,25 @@ def run_serving(args):
             alone_s += st.kernel_s
             r["alone_s"] = st.kernel_s
             cases += r["max_cases"]
-        else:
-            key = "x".join(map(str, sorted(r["dims"])))  # p x q and q x p fold alike
-            assert r["answer"] == golden[key], (key, r["answer"])
     plan.close()
+    summary = serving_summary(out)
     line = {"metric": "8x8 chunk serving: chunk p99 latency (s) under a Poisson stream",
             "value": out["chunk_p99_s"], "unit": "s", "higher_is_better": False,
             "chunk_p50_s": out["chunk_p50_s"], "all_p50_s": out["all_p50_s"],
             "all_p99_s": out["all_p99_s"], "cases_per_s": out["cases_per_s"],
             "nodes_per_s": out["nodes_per_s"], "wall_s": out["wall_s"],
             "alone_cases_per_s": cases / alone_s if alone_s else None,
+            "chunks_golden": summary["chunks_golden"],
             "ms_per_step": 1e3 * out["wall_s"], "scaling": "weak",
             "data": f"synthetic: serving_stream(seed={args.seed})",
             "config": {"workload": "8x8 MF_EXPANDED_N=36 50,000-case chunks + maps <= 5x6",
                        "requests": args.requests, "rate_per_s": args.rate,
-                       "chunks": sum(1 for r in out["results"] if r["kind"] == "chunk")},
-            "requests": [dict({k: r[k] for k in ("rid", "kind", "latency_s", "queue_s", "units")},
-                              arrival_s=q.arrival_s, alone_s=r.get("alone_s"))
-                         for r, q in zip(out["results"], reqs)],
-            "gpu_launches": None}
-    line.update(_gpu_common(args, clocks))
-    line["steps"] = 1
+                       "chunks": summary["chunks"]},
+            "requests": [{k: r.get(k) for k in ("rid", "kind", "latency_s", "queue_s", "units",
+                                                "arrival_s", "alone_s", "golden")}
+                         for r in out["results"]],
+            "gpu_launches": None, "n_gpus": 1, "steps": 1, "warmup": args.warmup,
+            "vs_baseline": None, "dtype": "u64", "clocks": out["clocks"], "note": summary["note"]}
     print(json.dumps(line), flush=True)
 
 
@@ -623,8 +712,11 @@ def run_nine(args):
 def run_profile_case(case: str):
     """One launch of each kernel on a small case, for ncu (a few seconds of
     GPU work, inputs ~28 MB): `sym-partial` counts the 433,131 7x7 cases from
-    24 to 30 cells (plain kernel, then batched); `lunnon` counts the 6x6 map
-    from its 18-leaf prefix states (plain, then batched)."""
+    24 to 30 cells (plain kernel, then batched); `sym-steady` the first 20,000
+    7x7 cases to completion (batched); `lunnon` counts the 6x6 map from its
+    18-leaf prefix states (plain, then batched); `wide` 300 9x9 cases on the
+    128-bit kernel; `serve` a 2,000-case 8x8 chunk and two maps through the
+    request server."""
     import numpy as np
     import torch
 
@@ -657,6 +749,22 @@ def run_profile_case(case: str):
         for mode in ("plain", "batched"):
             count, _, _ = plan.count(18, mode)
             assert count == 123912532224
+    elif case == "wide":
+        # the 128-bit kernel on the first 300 9x9 5x5-centre cases at 44 cells
+        plan = mf.SymPlan(9, 44, center_n=5)
+        golden = json.loads((ROOT / "tests" / "golden" / "reference_counts.json").read_text())
+        ans, _ = plan.solve(300, 0, "batched")
+        assert ans == golden["sym9"]["9x9_c5_d44_first300"]["count"]
+    elif case == "serve":
+        # the request server on one 8x8 chunk of 2,000 depth-36 cases and two maps
+        from map_folding_gb300.serving import Server
+
+        with Server() as srv:
+            ids = [srv.submit_sym(8, 36, 0, 2000), srv.submit_lunnon((4, 5)),
+                   srv.submit_lunnon((3, 6))]
+            got = [srv.wait(r)[0] for r in ids]
+        golden = json.loads((ROOT / "tests" / "golden" / "reference_counts.json").read_text())
+        assert got[1] == golden["lunnon"]["4x5"] and got[2] == golden["lunnon"]["3x6"]
     else:
         raise SystemExit(f"unknown profile case {case}")
     torch.cuda.synchronize()
@@ -669,10 +777,13 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    # The plain one-thread-per-case kernel needs ~500 s for the 7x7 count (its
-    # heaviest case runs on one thread), so it is timed only on request.
-    ap.add_argument("--plain", action="store_true", default=False)
+    # The plain one-thread-per-case kernel needs ~430 s for the 7x7 count (its
+    # heaviest case runs on one thread); it runs once, after the timed steps.
+    ap.add_argument("--plain", action="store_true", default=True)
     ap.add_argument("--no-plain", dest="plain", action="store_false")
+    ap.add_argument("--no-serving", dest="serving", action="store_false", default=True,
+                    help="7x7: skip the short serving-stream sub-record")
+    ap.add_argument("--e2e-steps", type=int, default=3, help="7x7: end-to-end repeats")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-case", default="", help="run one small case for ncu and exit")
     # Supplementary workloads, one JSON line each; the default is the 7x7 count.
