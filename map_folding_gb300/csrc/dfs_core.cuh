@@ -22,21 +22,47 @@ __device__ __forceinline__ uint64_t low_bits(int k) {
     return k >= 64 ? ~0ULL : ((1ULL << k) - 1ULL);
 }
 
-// Per-thread byte array in shared memory.  Byte j of thread t lives in
-// 32-bit word (j/4)*TPB + t, so a warp's 32 lanes always address 32
-// different banks, whatever indices they touch.
+// Per-thread byte array in shared memory, laid out so that a warp's 32 lanes
+// always address 32 different banks, whatever indices they touch.
+//
+// CTAs of a multiple of 128 threads (the 64-bit kernels): each group of four
+// warps shares 128-byte rows, row j holding byte j of all 128 threads --
+// lane l of warp w at byte 4*l + w, so lane l always reads bank l.  Byte j of
+// a thread is then at its base + 128*j: one shift-add per access, which the
+// walks make twice per step.  Other CTA sizes (the 64-thread 128-bit
+// kernel): byte j of thread t in 32-bit word (j/4)*TPB + t.
 template <int TPB>
 struct List {
-    uint8_t *base;  // smem + 4 * threadIdx.x
-    __device__ __forceinline__ int get(int j) const { return base[(j & ~3) * TPB + (j & 3)]; }
-    __device__ __forceinline__ void put(int j, int v) const {
-        base[(j & ~3) * TPB + (j & 3)] = static_cast<uint8_t>(v);
+    static constexpr bool kRows = TPB % 128 == 0;
+    uint8_t *base;  // this thread's byte 0
+    // The list of the calling thread in an area of `bytes` bytes per thread.
+    __device__ static List at(uint8_t *area, int bytes) {
+        const int t = threadIdx.x;
+        if constexpr (kRows) return List{area + (t >> 7) * bytes * 128 + 4 * (t & 31) + ((t >> 5) & 3)};
+        else return List{area + 4 * t};
     }
+    __device__ __forceinline__ int offset(int j) const {
+        if constexpr (kRows) return j << 7;
+        else return (j & ~3) * TPB + (j & 3);
+    }
+    __device__ __forceinline__ int get(int j) const { return base[offset(j)]; }
+    __device__ __forceinline__ void put(int j, int v) const { base[offset(j)] = static_cast<uint8_t>(v); }
+    // Bytes 4w .. 4w+3 as one little-endian word.
     __device__ __forceinline__ uint32_t word(int w) const {
-        return reinterpret_cast<const uint32_t *>(base)[w * TPB];
+        if constexpr (kRows) {
+            return uint32_t(get(4 * w)) | uint32_t(get(4 * w + 1)) << 8 |
+                   uint32_t(get(4 * w + 2)) << 16 | uint32_t(get(4 * w + 3)) << 24;
+        } else {
+            return reinterpret_cast<const uint32_t *>(base)[w * TPB];
+        }
     }
     __device__ __forceinline__ void set_word(int w, uint32_t v) const {
-        reinterpret_cast<uint32_t *>(base)[w * TPB] = v;
+        if constexpr (kRows) {
+#pragma unroll
+            for (int b = 0; b < 4; ++b) put(4 * w + b, int((v >> (8 * b)) & 0xffu));
+        } else {
+            reinterpret_cast<uint32_t *>(base)[w * TPB] = v;
+        }
     }
 };
 
@@ -64,48 +90,60 @@ __device__ __forceinline__ bool list_valid(const List<TPB> &L, int placed) {
 
 // ------------------------------------------------------------- rules -----
 
+// 1 << m with PTX shift semantics: 0 for m >= 64 (a walk may pass through
+// position 64, the last leaf of a 64-leaf map, which is never a gap).
+__device__ __forceinline__ uint64_t bit64(int m) {
+    uint64_t r;
+    asm("shl.b64 %0, %1, %2;" : "=l"(r) : "l"(1ULL), "r"(m));
+    return r;
+}
+
 // sym_fold.cpp:179-204: positions j < i after which cell i may follow in the
 // stack.  For each edge page whose neighbour `other` of i is placed, walk the
 // cycle from `other`, hopping over every placed partner pair, and keep the
-// positions landed on; AND the pages.  The pages' walks run as one flat loop
-// (a lane moves on to its next page inside the same loop), so a warp waits
-// for its longest lane's total walk, not for the sum of per-page maxima.
-// Both kinds of iteration -- starting a page and stepping along it -- end in
-// the same tail (mark the landed position, read its successor), so in a warp
-// whose lanes are at different kinds only the short heads diverge.  The pages
-// to walk for cell i are fixed by i alone and come packed from a per-cell
-// table: byte k = page << 6 | neighbour, `count` entries.
+// positions landed on; AND the pages.
+//
+// The pages are walked two at a time, side by side in one loop (on the
+// spiral numbering every cell has at most two placed neighbours, so that is
+// one pass): two independent dependent-load chains per lane instead of one,
+// and no page-start logic inside the loop.  A chain that has come back to its
+// start keeps stepping until the other one has too, which changes nothing:
+// from `other` the walk goes to L[other] again (other's partner on this page
+// is i itself, never placed), so it retraces the same positions.  With one
+// page the second chain is a copy of the first.  The pages to walk for cell i
+// come packed from a per-cell table: byte k = page << 6 | neighbour (so the
+// page's 64-byte row starts at byte & 0xC0), `count` entries.
 struct SymRules {
     const uint8_t *edge;     // 4 pages x 64, shared memory
     const uint32_t *pages;   // per cell: its placed-neighbour pages, packed
     const uint8_t *count;    // per cell: how many
-    template <int TPB>
-    __device__ __forceinline__ uint64_t gaps(const List<TPB> &L, int i,
+    template <class List>
+    __device__ __forceinline__ uint64_t gaps(const List &L, int i,
                                              unsigned long long &nodes) const {
         ++nodes;
         uint64_t good = low_bits(i);
         uint32_t q = pages[i];
-        int left = count[i];
-        const uint8_t *e = edge;
-        uint64_t allowed = ~0ULL;
-        int other = 0, j = 0;
-        for (;;) {
-            int x;
-            if (j == other) {  // current page finished (or none started)
-                good &= allowed;
-                if (!good || !left) break;
-                --left;
-                other = q & 63;
-                e = edge + ((q >> 6) & 3) * kSymCells;
-                q >>= 8;
-                allowed = 0;
-                x = other;
-            } else {
-                const int partner = e[j];
-                x = partner < i ? partner : j;
+        for (int left = count[i]; left > 0 && good; left -= 2, q >>= 16) {
+            const uint32_t qb = left > 1 ? (q >> 8) : q;
+            const int oA = q & 63, oB = qb & 63;
+            const uint8_t *eA = edge + (q & 0xC0);
+            const uint8_t *eB = edge + (qb & 0xC0);
+            uint64_t aA = 1ULL << oA, aB = 1ULL << oB;
+            int jA = L.get(oA), jB = L.get(oB);
+            bool dA = jA == oA, dB = jB == oB;
+            while (!(dA && dB)) {
+                const int pA = eA[jA];
+                const int pB = eB[jB];
+                const int xA = pA < i ? pA : jA;
+                const int xB = pB < i ? pB : jB;
+                aA |= 1ULL << xA;
+                aB |= 1ULL << xB;
+                jA = L.get(xA);
+                jB = L.get(xB);
+                dA |= jA == oA;
+                dB |= jB == oB;
             }
-            allowed |= 1ULL << x;
-            j = L.get(x);
+            good &= aA & aB;
         }
         return good;
     }
@@ -118,37 +156,48 @@ struct SymRules {
 // position 0..l-1 is a gap.  Position 0 (insert on top of the sentinel) is
 // dropped for l >= 2: it makes b[0] = l != 1 and the normal-form filter
 // (mf.c:83) would prune the whole subtree.  `nodes` counts the insertions
-// the reference loop would make (mf.c:136-142), position 0 included.  As for
-// sym, the dimensions' walks run as one flat loop.
+// the reference loop would make (mf.c:136-142), position 0 included.
+//
+// As for sym, the dimensions are walked two at a time side by side.  Setting
+// b[l] = l first (leaf l is not placed, so its slot is free until it is
+// inserted) makes every walk periodic: after reaching l it goes on to
+// d[l][b[l]] = d[l][l], its first position, and retraces itself, so a chain
+// that is done can keep stepping while the other finishes.  Bit l, picked up
+// on the way through, is not a position and is masked off.
 struct LunnonRules {
     const uint8_t *table;  // [dim][n+1][n+1]
     int n;
     int dim;
-    template <int TPB>
-    __device__ __forceinline__ uint64_t gaps(const List<TPB> &L, int l,
+    template <class List>
+    __device__ __forceinline__ uint64_t gaps(const List &L, int l,
                                              unsigned long long &nodes) const {
         const int w = n + 1;
-        uint64_t mask = ~0ULL, walked = ~0ULL;
-        int bound = 0, d = -1, m = l;
-        const uint8_t *row = table;
-        for (;;) {
-            if (m == l) {  // current dimension finished (or none started)
-                mask &= walked;
-                if (!mask) break;
-                int first = l;
-                while (++d < dim) {
-                    row = table + (d * w + l) * w;
-                    first = row[l];
-                    if (first != l) break;
-                }
-                if (d >= dim) break;
-                ++bound;
-                m = first;
-                walked = 0;
-                continue;
+        uint64_t mask = low_bits(l);
+        int bound = 0, d = 0;
+        L.put(l, l);
+        while (mask) {
+            const uint8_t *rA = nullptr, *rB = nullptr;
+            for (; d < dim && !rB; ++d) {
+                const uint8_t *row = table + (d * w + l) * w;
+                if (row[l] == l) continue;  // unconstrained dimension
+                if (!rA) rA = row;
+                else rB = row;
             }
-            walked |= 1ULL << m;
-            m = row[L.get(m)];
+            if (!rA) break;
+            if (!rB) rB = rA;
+            ++bound;
+            int mA = rA[l], mB = rB[l];
+            uint64_t wA = 0, wB = 0;
+            bool dA = false, dB = false;
+            while (!(dA && dB)) {
+                wA |= bit64(mA);
+                wB |= bit64(mB);
+                dA |= mA == l;
+                dB |= mB == l;
+                mA = rA[L.get(mA)];
+                mB = rB[L.get(mB)];
+            }
+            mask &= wA & wB;
         }
         if (!bound) mask = low_bits(l);
         nodes += __popcll(mask);
@@ -159,98 +208,113 @@ struct LunnonRules {
 
 // ------------------------------------------------------------- stacks ----
 
-// Per-level search state: the untried positions (mask) and the position the
-// level's item was inserted after (chosen).  Levels are stored relative to
-// `base`, the unit's first level.
+// Per-level search state, one 64-bit mask per level: the position the
+// level's item is inserted after is the mask's lowest set bit, and the
+// higher bits are its untried siblings.  (No separate pick byte: the pick is
+// a count-trailing-zeros away, one shared-memory store less per insertion.)
+// Levels are stored relative to `base`, the unit's first level.
 template <int TPB, int LEVELS>
 struct SmemStack {
     static constexpr int kLevels = LEVELS;
     uint64_t *mask;  // &s_mask[threadIdx.x], level k at mask[k * TPB]
-    List<TPB> chosen;
     int base;
     __device__ __forceinline__ uint64_t get(int lvl) const { return mask[(lvl - base) * TPB]; }
     __device__ __forceinline__ void set(int lvl, uint64_t v) const { mask[(lvl - base) * TPB] = v; }
-    __device__ __forceinline__ int pick(int lvl) const { return chosen.get(lvl - base); }
-    __device__ __forceinline__ void set_pick(int lvl, int j) const { chosen.put(lvl - base, j); }
 };
 
 struct LocalStack {
     static constexpr int kLevels = kLocalLevels;
     uint64_t mask[kLocalLevels];
-    uint8_t chosen[kLocalLevels];
     int base;
     __device__ __forceinline__ uint64_t get(int lvl) const { return mask[lvl - base]; }
     __device__ __forceinline__ void set(int lvl, uint64_t v) { mask[lvl - base] = v; }
-    __device__ __forceinline__ int pick(int lvl) const { return chosen[lvl - base]; }
-    __device__ __forceinline__ void set_pick(int lvl, int j) { chosen[lvl - base] = uint8_t(j); }
 };
+
+__device__ __forceinline__ int low_bit(uint64_t m) { return __ffsll(static_cast<long long>(m)) - 1; }
 
 // ---------------------------------------------------------- DFS core -----
 //
 // Lockstep form: in every round each busy lane evaluates exactly one node
 // (one gaps() call), so a warp's lanes run the expensive walk together no
 // matter where each is in its own tree.  Between evaluations a lane
-// `advance`s: it backtracks over exhausted levels and inserts its next
-// untried item, which names the level to evaluate next.
+// advances: it backtracks over exhausted levels and inserts its next untried
+// item, which names the level to evaluate next.
 
-// Position the lane on its next node.  Items root..lvl-1 are inserted and
-// S[lvl] holds lvl's untried positions.  Backtracks over exhausted levels,
-// inserts item lvl after the next untried position and returns lvl + 1 (the
-// level to evaluate), or -1 when the unit's subtree is exhausted.
-template <class Stk, int TPB>
-__device__ __forceinline__ int advance(const List<TPB> &L, Stk &S, int &lvl, int root) {
-    for (;;) {
-        const uint64_t cur = S.get(lvl);
-        if (cur == 0) {
-            if (lvl == root) return -1;
-            --lvl;
-            L.put(S.pick(lvl), L.get(lvl));  // detach item lvl
-            continue;
-        }
-        const int j = __ffsll(static_cast<long long>(cur)) - 1;
-        S.set(lvl, cur & (cur - 1));
-        L.put(lvl, L.get(j));  // insert item lvl after j
-        L.put(j, lvl);
-        S.set_pick(lvl, j);
-        return lvl + 1;
-    }
+// Insert item lvl after the lowest position of `cur` (cur != 0) and record
+// cur as the level's mask; returns the level to evaluate next.
+template <class Stk, class List>
+__device__ __forceinline__ int descend(const List &L, Stk &S, int lvl, uint64_t cur) {
+    const int j = low_bit(cur);
+    S.set(lvl, cur);
+    L.put(lvl, L.get(j));  // insert item lvl after j
+    L.put(j, lvl);
+    return lvl + 1;
+}
+
+// Start a split item: S[root] holds the untried positions of level root (never
+// empty), no item of level root is inserted yet.  Returns root + 1.
+template <class Stk, class List>
+__device__ __forceinline__ int advance(const List &L, Stk &S, int &lvl, int root) {
+    lvl = root;
+    return descend(L, S, root, S.get(root));
 }
 
 // Consume the evaluation g of level `eval` and advance to the next node, with
-// g handed over in a register (a level that was just evaluated starts from g
-// instead of storing it to the stack and loading it straight back).  The
-// last level is never entered: its positions are counted and the item above
-// it detached again.  Returns the next level to evaluate, or -1 when the
-// unit's subtree is exhausted (or a fresh unit had nothing left to place).
-template <class Stk, int TPB>
-__device__ __forceinline__ int apply_advance(const List<TPB> &L, Stk &S, int &lvl, int eval,
+// g handed over in a register.  Items root..eval-1 are inserted.  The last
+// level is never entered: its positions are counted.  After a counted last
+// level or a dead end the item above is detached and its next sibling, if
+// any, inserted; exhausted levels are backtracked over.  Returns the next
+// level to evaluate, or -1 when the unit's subtree is exhausted (or a fresh
+// unit had nothing left to place).
+template <class Stk, class List>
+__device__ __forceinline__ int apply_advance(const List &L, Stk &S, int &lvl, int eval,
                                              int root, int last, bool fresh, uint64_t g,
                                              unsigned long long &leaves) {
-    uint64_t cur;
-    if (eval == last) {
-        leaves += __popcll(g);
-        if (fresh) return -1;  // a unit with nothing left to place
-        L.put(S.pick(lvl), L.get(lvl));  // detach item lvl (= eval - 1)
-        cur = S.get(lvl);
-    } else {
+    if (eval != last && g) {
         lvl = eval;
-        cur = g;
+        return descend(L, S, lvl, g);
     }
+    if (eval == last) leaves += __popcll(g);
+    if (fresh) return -1;  // a fresh unit: nothing above it to go back to
+    lvl = eval - 1;
     for (;;) {
-        if (cur == 0) {
-            if (lvl == root) return -1;
-            --lvl;
-            L.put(S.pick(lvl), L.get(lvl));  // detach item lvl
-            cur = S.get(lvl);
-            continue;
-        }
-        const int j = __ffsll(static_cast<long long>(cur)) - 1;
-        S.set(lvl, cur & (cur - 1));
-        L.put(lvl, L.get(j));  // insert item lvl after j
-        L.put(j, lvl);
-        S.set_pick(lvl, j);
-        return lvl + 1;
+        const uint64_t m = S.get(lvl);
+        L.put(low_bit(m), L.get(lvl));  // detach item lvl
+        const uint64_t rest = m & (m - 1);
+        if (rest) return descend(L, S, lvl, rest);
+        if (lvl == root) return -1;
+        --lvl;
     }
+}
+
+// Donation (splitting a lane's subtree on the device).  Items root..lvl are
+// inserted.  The shallowest level s with untried siblings, and those
+// siblings (0 if no level has any).
+template <class Stk>
+__device__ __forceinline__ uint64_t shallowest_siblings(const Stk &S, int root, int lvl, int &s) {
+    s = root;
+    uint64_t m = S.get(s);
+    while (s < lvl && (m & (m - 1)) == 0) m = S.get(++s);
+    return m & (m - 1);
+}
+
+// Detach items lvl..s, leaving the list as it was before item s was placed.
+template <class Stk, class List>
+__device__ __forceinline__ void roll_back(const List &L, const Stk &S, int s, int lvl) {
+    for (int l = lvl; l >= s; --l) L.put(low_bit(S.get(l)), L.get(l));
+}
+
+// Re-insert items s..lvl after roll_back; level s keeps only its current
+// pick (its untried siblings have been given away).
+template <class Stk, class List>
+__device__ __forceinline__ void replay_keeping_pick(const List &L, Stk &S, int s, int lvl) {
+    for (int l = s; l <= lvl; ++l) {
+        const int j = low_bit(S.get(l));
+        L.put(l, L.get(j));
+        L.put(j, l);
+    }
+    const uint64_t ms = S.get(s);
+    S.set(s, ms & (~ms + 1));
 }
 
 template <int TPB, int WORDS>
@@ -276,20 +340,18 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
     return v;
 }
 
-// Shared-memory carve-up of one CTA: [tables][lists][mask stack][picks].
+// Shared-memory carve-up of one CTA: [tables][lists][mask stack].
 template <int TPB, int WORDS, int LEVELS>
 struct Carve {
     static constexpr size_t kList = size_t(WORDS) * 4 * TPB;
     static constexpr size_t kMask = size_t(LEVELS) * 8 * TPB;
-    static constexpr size_t kPick = size_t((LEVELS + 3) / 4) * 4 * TPB;
-    static constexpr size_t kThreadBytes = kList + kMask + kPick;
+    static constexpr size_t kThreadBytes = kList + kMask;
     __device__ static List<TPB> list(uint8_t *smem, size_t tables) {
-        return List<TPB>{smem + tables + 4 * threadIdx.x};
+        return List<TPB>::at(smem + tables, 4 * WORDS);
     }
     __device__ static SmemStack<TPB, LEVELS> stack(uint8_t *smem, size_t tables) {
         SmemStack<TPB, LEVELS> s;
         s.mask = reinterpret_cast<uint64_t *>(smem + tables + kList) + threadIdx.x;
-        s.chosen = List<TPB>{smem + tables + kList + kMask + 4 * threadIdx.x};
         s.base = 0;
         return s;
     }
@@ -300,7 +362,7 @@ struct Carve<TPB, WORDS, 0> {  // local-memory stack
     static constexpr size_t kList = size_t(WORDS) * 4 * TPB;
     static constexpr size_t kThreadBytes = kList;
     __device__ static List<TPB> list(uint8_t *smem, size_t tables) {
-        return List<TPB>{smem + tables + 4 * threadIdx.x};
+        return List<TPB>::at(smem + tables, 4 * WORDS);
     }
 };
 

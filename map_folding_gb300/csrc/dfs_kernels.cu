@@ -240,11 +240,7 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
     // level, copies it out, replays, and publishes.
     auto donate = [&]() {
         int s = root;
-        uint64_t m = 0;
-        if (busy && !fresh) {
-            while (s < lvl && S.get(s) == 0) ++s;
-            m = S.get(s);
-        }
+        const uint64_t m = busy && !fresh ? shallowest_siblings(S, root, lvl, s) : 0;
         const bool can = busy && !fresh && m != 0 && last - s >= kMinSplitHeight;
         const unsigned donors = __ballot_sync(kFull, can);
         if (!donors) return;
@@ -252,7 +248,7 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
         const int got = ring_claim(Q, &Q.hdr->spawn_tail, __popc(donors), false, first);
         const int rank = __popc(donors & lt_mask);
         if (!can || rank >= got) return;
-        for (int l = lvl; l >= s; --l) L.put(S.pick(l), L.get(l));
+        roll_back(L, S, s, lvl);
         uint32_t w[24];
 #pragma unroll
         for (int k = 0; k < 24; ++k) w[k] = 0;
@@ -262,12 +258,7 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
         w[18] = uint32_t(m);
         w[19] = uint32_t(m >> 32);
         w[20] = uint32_t(s);
-        for (int l = s; l <= lvl; ++l) {
-            const int j = S.pick(l);
-            L.put(l, L.get(j));
-            L.put(j, l);
-        }
-        S.set(s, 0);
+        replay_keeping_pick(L, S, s, lvl);
         ring_put(Q, first + rank, w);
     };
 
@@ -439,7 +430,7 @@ __global__ void __launch_bounds__(TPB)
 // Shared memory: the maps' neighbour tables and their instance records
 // (meta_bytes in all, records at inst_offset), then the carve.
 template <int TPB, int LEVELS>
-__global__ void __launch_bounds__(TPB)
+__global__ void __launch_bounds__(TPB, 768 / TPB)  // <= 85 registers: six 128-thread CTAs per SM
     lunnon_batched_kernel(const uint8_t *__restrict__ meta, uint32_t meta_bytes,
                           uint32_t inst_offset, LunnonSource src, unsigned long long num,
                           unsigned long long *counts, unsigned long long *nodes_out, Queue Q,

@@ -326,11 +326,7 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
             // every lane when lanes are idle, else the oldest request's lanes
             // to keep its stock of split items.
             int s = root;
-            uint64_t m = 0;
-            if (busy && !fresh) {
-                while (s < lvl && S.get(s) == 0) ++s;
-                m = S.get(s);
-            }
+            const uint64_t m = busy && !fresh ? shallowest_siblings(S, root, lvl, s) : 0;
             const bool can = busy && !fresh && m != 0 && last - s >= kMinSplitHeight &&
                              (want > 0 || my_seq == oldest);
             const unsigned donors = __ballot_sync(kFull, can);
@@ -339,7 +335,7 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
                 const int got = ring_claim(A.Q, &A.Q.hdr->spawn_tail, __popc(donors), false, first);
                 const int rank = __popc(donors & lt_mask);
                 if (can && rank < got) {
-                    for (int l = lvl; l >= s; --l) L.put(S.pick(l), L.get(l));
+                    roll_back(L, S, s, lvl);
                     uint32_t w[24];
 #pragma unroll
                     for (int k = 0; k < 24; ++k) w[k] = 0;
@@ -351,12 +347,7 @@ __global__ void __launch_bounds__(TPB) serve_kernel(ServeArgs A) {
                     w[20] = uint32_t(s);
                     w[22] = uint32_t(mult);
                     w[23] = uint32_t(mult >> 32);
-                    for (int l = s; l <= lvl; ++l) {
-                        const int j = S.pick(l);
-                        L.put(l, L.get(j));
-                        L.put(j, l);
-                    }
-                    S.set(s, 0);
+                    replay_keeping_pick(L, S, s, lvl);
                     atomicAdd(reinterpret_cast<unsigned long long *>(A.pending + slot), 1ULL);
                     ring_put(A.Q, first + rank, w);
                 }

@@ -68,8 +68,10 @@ __device__ __forceinline__ void stage_wide_tables(uint8_t *smem, const uint8_t *
     }
 }
 
-// get_good with 128-bit masks (sym_fold9.cpp:286-312), in the unified form of
-// SymRules::gaps.
+// get_good with 128-bit masks (sym_fold9.cpp:286-312), in the two-chain form
+// of SymRules::gaps: the (at most two) placed-neighbour pages of cell i are
+// walked side by side, a chain that is back at its start retracing itself
+// until the other is done.
 struct SymRulesW {
     const uint8_t *edge;
     const uint64_t *pages;
@@ -80,28 +82,30 @@ struct SymRulesW {
         ++nodes;
         Mask128 good = w_low_bits(i);
         uint64_t q = pages[i];
-        int left = count[i];
-        const uint8_t *e = edge;
-        Mask128 allowed{~0ULL, ~0ULL};
-        int other = 0, j = 0;
-        for (;;) {
-            int x;
-            if (j == other) {  // current page finished (or none started)
-                good.lo &= allowed.lo;
-                good.hi &= allowed.hi;
-                if (w_zero(good) || !left) break;
-                --left;
-                other = int(q & 127);
-                e = edge + int((q >> 7) & 3) * kWideCells;
-                q >>= 9;
-                allowed = Mask128{0, 0};
-                x = other;
-            } else {
-                const int partner = e[j];
-                x = partner < i ? partner : j;
+        for (int left = count[i]; left > 0 && !w_zero(good); left -= 2, q >>= 18) {
+            const uint64_t qb = left > 1 ? (q >> 9) : q;
+            const int oA = int(q & 127), oB = int(qb & 127);
+            const uint8_t *eA = edge + int((q >> 7) & 3) * kWideCells;
+            const uint8_t *eB = edge + int((qb >> 7) & 3) * kWideCells;
+            Mask128 aA{0, 0}, aB{0, 0};
+            w_set(aA, oA);
+            w_set(aB, oB);
+            int jA = L.get(oA), jB = L.get(oB);
+            bool dA = jA == oA, dB = jB == oB;
+            while (!(dA && dB)) {
+                const int pA = eA[jA];
+                const int pB = eB[jB];
+                const int xA = pA < i ? pA : jA;
+                const int xB = pB < i ? pB : jB;
+                w_set(aA, xA);
+                w_set(aB, xB);
+                jA = L.get(xA);
+                jB = L.get(xB);
+                dA |= jA == oA;
+                dB |= jB == oB;
             }
-            w_set(allowed, x);
-            j = L.get(x);
+            good.lo &= aA.lo & aB.lo;
+            good.hi &= aA.hi & aB.hi;
         }
         return good;
     }
