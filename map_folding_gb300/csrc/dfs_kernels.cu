@@ -5,11 +5,13 @@
 // over spiral cells, sym_fold.cpp:206-217), grown one item per level by
 // inserting item `lvl` after a chosen position, with the set of admissible
 // positions recomputed at every level by walking the list.  The engine below
-// keeps that list per thread in shared memory (byte per item, word-interleaved
-// across the CTA so a warp never has a bank conflict), keeps the per-level
-// choices as a 64-bit mask stack (in shared memory when the search is at most
-// kSmemLevels deep, else in local memory) instead of the reference's gap[]
-// array, and counts the last level with a popcount.  Gap rules:
+// keeps that list per thread in shared memory (byte per item, in 128-byte
+// rows shared by four warps so a warp never has a bank conflict), keeps the
+// per-level choices as a 64-bit mask stack whose lowest bit is the current
+// pick (in shared memory when the search is at most 48 levels deep, else in
+// local memory) instead of the reference's gap[] array, walks a node's two
+// constraint chains side by side, and counts the last level with a popcount.
+// Gap rules:
 //   LunnonRules  -- mf.c:88-124 as a bitwise AND of per-dimension walk masks
 //   SymRules     -- sym_fold.cpp:179-204 (get_good)
 // Kernels:
