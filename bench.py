@@ -709,6 +709,85 @@ def run_nine(args):
     print(json.dumps(line), flush=True)
 
 
+def _timed_run(cmd, timeout_s=900):
+    t0 = time.perf_counter()
+    res = subprocess.run([str(c) for c in cmd], capture_output=True, text=True, timeout=timeout_s)
+    return time.perf_counter() - t0, res
+
+
+def run_reference_gpu(args):
+    """The reference's own GPU drivers on this GPU next to the engine: the
+    unmodified gpu_folding.cu (one thread per prefix state) and
+    gpu_folding_v2.cu (batched producer/worker solve_kernel), built here with
+    nvcc for sm_103a from the copies oracle/Makefile stages into
+    baseline/_ref/src/, run through their own CLIs on 5x5 at depth 15 and
+    6x6 at depth 18 (each generates its own prefix states), wall-timed as
+    processes; the engine's drop-in bin/gpu_folding on the same arguments,
+    wall-timed the same way, and its kernel time through the C ABI.  Every
+    count is checked against the reference's count."""
+    import map_folding_gb300 as mf
+    from map_folding_gb300 import build as mfbuild
+
+    src = ROOT / "baseline" / "_ref" / "src"
+    if not (src / "gpu_folding.cu").exists():
+        print(json.dumps({"impl": "reference-gpu", "unavailable":
+                          "baseline/_ref/src has no staged reference CUDA sources "
+                          "(make -C oracle gpu_src needs the reference checkout)"}), flush=True)
+        return
+    out_dir = ROOT / "baseline" / "_ref" / "bin"
+    out_dir.mkdir(parents=True, exist_ok=True)
+    for name in ("gpu_folding", "gpu_folding_v2"):
+        subprocess.run(["nvcc", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-o",
+                        str(out_dir / name), str(src / f"{name}.cu")], check=True,
+                       capture_output=True)
+    if not mfbuild.LIB.exists():
+        mfbuild.build()
+    ours = mfbuild.BIN / "gpu_folding"
+    golden = _golden_lunnon()
+    rows = []
+    with ClockSampler(0) as clocks:
+        for grid, depth in ((5, 15), (6, 18)):
+            want = golden[f"{grid}x{grid}"]
+            row = {"map": f"{grid}x{grid}", "depth": depth}
+            el, res = _timed_run([out_dir / "gpu_folding", grid, depth])
+            got = int(res.stdout.strip().splitlines()[-1].split(":")[-1])
+            assert res.returncode == 0 and got == want, ("gpu_folding", grid, got)
+            row["reference_gpu_folding_s"] = el
+            el, res = _timed_run([out_dir / "gpu_folding_v2", grid, depth, 5000, 128, 8, 1])
+            got = int(res.stdout.strip().splitlines()[-1])
+            assert res.returncode == 0 and got == want, ("gpu_folding_v2", grid, got)
+            kv = dict(tok.split("=", 1) for tok in res.stderr.split() if "=" in tok)
+            row["reference_gpu_folding_v2_s"] = el
+            row["reference_gpu_folding_v2_solve_s"] = float(kv.get("solve_s", "nan"))
+            for mode in ("batched", "plain"):
+                best = None
+                for _ in range(max(1, args.steps)):
+                    el, res = _timed_run([ours, grid, depth, mode])
+                    got = int(res.stdout.strip().splitlines()[-1].split(":")[-1])
+                    assert res.returncode == 0 and got == want, ("ours", mode, grid, got)
+                    best = el if best is None else min(best, el)
+                row[f"ours_{mode}_process_s"] = best
+                plan = mf.LunnonPlan((grid, grid))
+                c, _, st = plan.count(depth, mode)
+                plan.close()
+                assert c == want
+                row[f"ours_{mode}_kernel_s"] = st.kernel_s
+            row["process_speedup_vs_gpu_folding"] = (row["reference_gpu_folding_s"] /
+                                                     row["ours_batched_process_s"])
+            row["process_speedup_vs_gpu_folding_v2"] = (row["reference_gpu_folding_v2_s"] /
+                                                        row["ours_batched_process_s"])
+            rows.append(row)
+    line = {"metric": "Lunnon whole-map wall time: the reference's own GPU drivers vs the engine, same GPU",
+            "value": rows[-1]["process_speedup_vs_gpu_folding_v2"], "unit": "x (gpu_folding_v2 / ours, 6x6@18)",
+            "higher_is_better": True, "data": "synthetic: exhaustive map counts",
+            "config": {"workload": "gpu_folding / gpu_folding_v2 (reference, unmodified, nvcc sm_103a) "
+                                   "vs bin/gpu_folding on 5x5@15 and 6x6@18",
+                       "v2_args": "batch_size 5000, threads_per_block 128, blocks_per_sm 8, max_gpus 1"},
+            "maps": rows, "n_gpus": 1, "steps": args.steps, "warmup": 0, "vs_baseline": None,
+            "dtype": "u64", "clocks": clocks.summary(), "gpu_launches": None}
+    print(json.dumps(line), flush=True)
+
+
 def run_profile_case(case: str):
     """One launch of each kernel on a small case, for ncu (a few seconds of
     GPU work, inputs ~28 MB): `sym-partial` counts the 433,131 7x7 cases from
@@ -788,7 +867,8 @@ def main():
     ap.add_argument("--profile-case", default="", help="run one small case for ncu and exit")
     # Supplementary workloads, one JSON line each; the default is the 7x7 count.
     ap.add_argument("--workload", default="7x7",
-                    choices=["7x7", "lunnon", "uneven", "serving", "chunk-plan", "9x9"])
+                    choices=["7x7", "lunnon", "uneven", "serving", "chunk-plan", "9x9",
+                             "reference-gpu"])
     ap.add_argument("--cost-depth", type=int, default=6, help="chunk-plan: lookahead depth")
     ap.add_argument("--requests", type=int, default=12, help="serving: requests in the stream")
     ap.add_argument("--rate", type=float, default=0.15, help="serving: Poisson arrivals per second")
@@ -808,6 +888,8 @@ def main():
         run_chunk_plan(args)
     elif args.workload == "9x9":
         run_nine(args)
+    elif args.workload == "reference-gpu":
+        run_reference_gpu(args)
     else:
         run_ours(args)
 

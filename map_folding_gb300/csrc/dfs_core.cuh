@@ -428,6 +428,84 @@ __device__ __forceinline__ void stage_sym_tables(uint8_t *smem, const uint8_t *_
     }
 }
 
+// The counting kernels precompute, per searched level i and per chain k (the
+// cell's first or second placed-neighbour page), the position the walk lands
+// on from each position j: hop[(i - first) * 128 + k * 64 + j] = j's partner
+// on that page if the partner is placed (< i), else j.  A walk step is then
+// one table byte and one list byte -- the compare-and-select of get_good's
+// `edge[j] < i` test is gone from the walk, which is bound by the integer
+// (ALU) pipe.  128 bytes per level: 3.2 KB for the 7x7 search from 24 cells.
+__host__ __device__ constexpr size_t sym_hop_bytes(int levels) {
+    return size_t(levels > 0 ? levels : 0) * 128;
+}
+
+template <int TPB>
+__device__ __forceinline__ void stage_sym_hops(uint8_t *hop, const uint8_t *tables, int first,
+                                               int levels) {
+    const uint32_t *pages = reinterpret_cast<const uint32_t *>(tables + 4 * kSymCells);
+    const uint8_t *count = tables + 8 * kSymCells;
+    for (int k = threadIdx.x; k < levels * 128; k += TPB) {
+        const int i = first + (k >> 7), chain = (k >> 6) & 1, j = k & 63;
+        const int c = count[i];
+        const uint32_t q = (chain && c > 1) ? (pages[i] >> 8) : pages[i];
+        const int p = tables[(q & 0xC0) + j];
+        hop[k] = uint8_t(c != 0 && p < i ? p : j);
+    }
+}
+
+// SymRules with the precomputed hop rows (levels first .. first + levels - 1).
+struct SymHopRules {
+    const uint8_t *hop;
+    const uint32_t *pages;
+    const uint8_t *count;
+    int first;
+    template <class List>
+    __device__ __forceinline__ uint64_t gaps(const List &L, int i,
+                                             unsigned long long &nodes) const {
+        ++nodes;
+        const uint32_t q = pages[i];
+        const int c = count[i];
+        if (c == 0) return low_bits(i);
+        const uint32_t qb = c > 1 ? (q >> 8) : q;
+        const int oA = q & 63, oB = qb & 63;
+        const uint8_t *hA = hop + (i - first) * 128;
+        const uint8_t *hB = hA + 64;
+        uint64_t aA = 1ULL << oA, aB = 1ULL << oB;
+        int jA = L.get(oA), jB = L.get(oB);
+        bool dA = jA == oA, dB = jB == oB;
+        while (!(dA && dB)) {
+            const int xA = hA[jA];
+            const int xB = hB[jB];
+            aA |= 1ULL << xA;
+            aB |= 1ULL << xB;
+            jA = L.get(xA);
+            jB = L.get(xB);
+            dA |= jA == oA;
+            dB |= jB == oB;
+        }
+        return low_bits(i) & aA & aB;
+    }
+};
+
+// Shared-memory size of the sym tables plus the hop rows of `levels` levels.
+__host__ __device__ constexpr size_t sym_tables_bytes(int levels) {
+    return 9 * kSymCells + sym_hop_bytes(levels);
+}
+
+// Stage the tables and the hop rows of levels first .. first + levels - 1
+// (ends with __syncthreads).
+template <int TPB>
+__device__ __forceinline__ SymHopRules stage_sym_hop_rules(uint8_t *smem,
+                                                           const uint8_t *__restrict__ edges,
+                                                           int first, int levels) {
+    stage_sym_tables<TPB>(smem, edges);
+    __syncthreads();
+    stage_sym_hops<TPB>(smem + 9 * kSymCells, smem, first, levels);
+    __syncthreads();
+    return SymHopRules{smem + 9 * kSymCells, reinterpret_cast<const uint32_t *>(smem + 4 * kSymCells),
+                       smem + 8 * kSymCells, first};
+}
+
 __device__ __forceinline__ SymRules sym_rules(const uint8_t *smem) {
     return SymRules{smem, reinterpret_cast<const uint32_t *>(smem + 4 * kSymCells),
                     smem + 8 * kSymCells};

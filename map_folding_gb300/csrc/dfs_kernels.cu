@@ -49,19 +49,19 @@ __global__ void __launch_bounds__(TPB)
                      unsigned long long *__restrict__ nodes_out) {
     extern __shared__ __align__(16) uint8_t smem[];
     using C = Carve<TPB, 16, LEVELS>;
-    stage_sym_tables<TPB>(smem, edges);
-    const List<TPB> L = C::list(smem, kSymTables);
+    const SymHopRules R = stage_sym_hop_rules<TPB>(smem, edges, start_i, stop_i - start_i);
+    const size_t tables = sym_tables_bytes(stop_i - start_i);
+    const List<TPB> L = C::list(smem, tables);
     typename StackOf<TPB, LEVELS>::type S;
-    init_stack<TPB, 16, LEVELS>(S, smem, kSymTables);
+    init_stack<TPB, 16, LEVELS>(S, smem, tables);
     const uint64_t unit = uint64_t(blockIdx.x) * TPB + threadIdx.x;
     const bool active = unit < num;
     if (active) load_list<TPB, 16>(L, cycles + unit * kSymCells, kSymCells);
-    __syncthreads();
 
     unsigned long long nodes = 0, leaves = 0;
     const bool bad = active && !list_valid(L, start_i);
     S.base = start_i;
-    run_units(sym_rules(smem), L, S, active && !bad, start_i, stop_i - 1, leaves, nodes);
+    run_units(R, L, S, active && !bad, start_i, stop_i - 1, leaves, nodes);
     if (active) counts[unit] = bad ? ~0ULL : leaves;
     if (nodes_out) {
         const unsigned long long s = warp_sum(nodes);
@@ -129,10 +129,11 @@ struct LunnonSource {
 
 // The persistent loop, in lockstep rounds.  Each round every busy lane
 // evaluates one node, consumes it and advances to its next node; a lane whose
-// unit is exhausted starts its next one at once from a one-unit-ahead
-// prefetch (the index is taken with an atomicAdd when the previous unit
-// starts, the record is loaded into registers at the next bookkeeping round,
-// so neither latency is paid when the unit is needed).  Every `period` rounds
+// unit is exhausted starts its next one at once: the next unit's index is
+// taken with an atomicAdd when the previous unit starts, so only the record
+// load is paid when the unit is needed (holding the record in registers
+// ahead of time cost 16-20 registers per thread for the whole search, which
+// the occupancy needs more).  Every `period` rounds
 // a warp does its bookkeeping: it reports finished units and its idle-lane
 // count, lets idle lanes take split items, and -- while fewer split items are
 // queued than lanes wait for work -- lets a few busy lanes give away their
@@ -160,12 +161,13 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
     uint32_t idle_rounds = 0, round = 0;
     int reported_idle = 0;  // lane 0: idle lanes this warp last reported
     bool ring_hint = false;  // warp-uniform: the split ring probably has items
-    const SymRules srules = sym_rules(s_tables);
+    const SymHopRules srules{s_tables + 9 * kSymCells,
+                             reinterpret_cast<const uint32_t *>(s_tables + 4 * kSymCells),
+                             s_tables + 8 * kSymCells, sym.start_i};
     LunnonRules lrules{s_tables, 0, 0};
 
     // Prefetch state: 0 = no initial unit left for this lane, 1 = index
-    // requested, 2 = record requested too.  The first indices come from one
-    // warp-aggregated atomicAdd.
+    // taken.  The first indices come from one warp-aggregated atomicAdd.
     unsigned long long pre_k = 0;
     {
         unsigned long long base = 0;
@@ -183,7 +185,6 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
             : reinterpret_cast<const uint4 *>(lun.states + pre_k * lun.stride);            \
         _Pragma("unroll") for (int q_ = 0; q_ < kVecs; ++q_) pre[q_] = __ldg(src_ + q_);   \
         if (!kSym) pre_owner = __ldg(lun.state_owner + pre_k);                             \
-        pre_stage = 2;                                                                     \
     } while (0)
 
     auto flush = [&]() {
@@ -269,7 +270,7 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
         // Start the prefetched unit on lanes whose search has ended.
         if (!busy && pre_stage != 0) {
             if (pre_k < num) {
-                if (pre_stage == 1) MF_FETCH_RECORD();
+                MF_FETCH_RECORD();
 #pragma unroll
                 for (int q = 0; q < kVecs; ++q) {
                     const uint32_t ws[4] = {pre[q].x, pre[q].y, pre[q].z, pre[q].w};
@@ -369,11 +370,6 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
         }
         if (!bookkeeping) continue;
         round = 0;
-        // Prefetched indices have long arrived: request their records.
-        if (pre_stage == 1) {
-            if (pre_k < num) MF_FETCH_RECORD();
-            else pre_stage = 0;
-        }
         const unsigned idle_mask = __ballot_sync(kFull, !busy);
         const unsigned long long f = warp_sum(finished);
         finished = 0;
@@ -419,11 +415,11 @@ __global__ void __launch_bounds__(TPB)
                        uint32_t period, uint32_t wait_limit) {
     extern __shared__ __align__(16) uint8_t smem[];
     using C = Carve<TPB, 16, LEVELS>;
-    stage_sym_tables<TPB>(smem, edges);
-    __syncthreads();
-    const List<TPB> L = C::list(smem, kSymTables);
+    stage_sym_hop_rules<TPB>(smem, edges, src.start_i, src.last - src.start_i + 1);
+    const size_t tables = sym_tables_bytes(src.last - src.start_i + 1);
+    const List<TPB> L = C::list(smem, tables);
     typename StackOf<TPB, LEVELS>::type S;
-    init_stack<TPB, 16, LEVELS>(S, smem, kSymTables);
+    init_stack<TPB, 16, LEVELS>(S, smem, tables);
     LunnonSource none{};
     persistent_loop<TPB, 16, true>(smem, nullptr, src, none, num, counts, nodes_out, Q, period,
                                    wait_limit, L, S);
@@ -432,7 +428,7 @@ __global__ void __launch_bounds__(TPB)
 // Shared memory: the maps' neighbour tables and their instance records
 // (meta_bytes in all, records at inst_offset), then the carve.
 template <int TPB, int LEVELS>
-__global__ void __launch_bounds__(TPB, 768 / TPB)  // <= 85 registers: six 128-thread CTAs per SM
+__global__ void __launch_bounds__(TPB)
     lunnon_batched_kernel(const uint8_t *__restrict__ meta, uint32_t meta_bytes,
                           uint32_t inst_offset, LunnonSource src, unsigned long long num,
                           unsigned long long *counts, unsigned long long *nodes_out, Queue Q,
@@ -573,7 +569,7 @@ cudaError_t launch_sym_plain(const uint8_t *d_edges, int start_i, int stop_i,
     constexpr int TPB = 128;
     const uint64_t blocks = (num + TPB - 1) / TPB;
     const int levels = pick_levels(stop_i - 1 - start_i);
-    const size_t tables = kSymTables;
+    const size_t tables = sym_tables_bytes(stop_i - start_i);
     auto *counts = reinterpret_cast<unsigned long long *>(d_counts);
     auto *nodes = reinterpret_cast<unsigned long long *>(d_nodes);
     int bpsm = 0;
@@ -639,7 +635,7 @@ cudaError_t launch_sym_batched(const uint8_t *d_edges, int start_i, int stop_i,
     const int sms = device_sm_count();
     const SymSource src{d_cycles, start_i, stop_i - 1};
     const int levels = pick_levels(stop_i - 1 - start_i, knobs.stack_mode == 1);
-    const size_t tables = kSymTables;
+    const size_t tables = sym_tables_bytes(stop_i - start_i);
     auto *counts = reinterpret_cast<unsigned long long *>(d_counts);
     auto *nodes = reinterpret_cast<unsigned long long *>(d_nodes);
     int bpsm = 0;
