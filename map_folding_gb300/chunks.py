@@ -217,9 +217,12 @@ def sweep(n: int = 8, threads: int = 16, expanded_n: int = 36,
           total_cases: int = TOTAL_8X8_DEPTH36_CASES, chunk_size: int = 100000,
           start_case: int = 0, chunk_count: int = 0, out: str = "",
           resume_existing: bool = False, mode: str = "batched", in_process: bool = True,
-          chunk_plan: list[tuple[int, int]] | None = None) -> dict:
+          chunk_plan: list[tuple[int, int]] | None = None, max_seconds: float = 0.0) -> dict:
     """modal_sym.py:152-236 on the local GPU.  With chunk_plan, the given
-    (start_case, max_cases) chunks run instead of equal-size ones."""
+    (start_case, max_cases) chunks run instead of equal-size ones.  With
+    max_seconds > 0 no new chunk starts once that much wall time has passed
+    (the rows written so far are the checkpoint; --resume-existing carries
+    on from them), so a long sweep can run as bounded sessions."""
     if chunk_plan is not None:
         inputs = [(int(s), int(m)) for s, m in chunk_plan]
         if chunk_count > 0:
@@ -261,6 +264,9 @@ def sweep(n: int = 8, threads: int = 16, expanded_n: int = 36,
     print(f"chunks={len(inputs)} chunk_size={chunk_size} out={out_path}", flush=True)
     with out_path.open("a", encoding="utf-8") as f:
         for s, m in inputs:
+            if max_seconds > 0 and time.perf_counter() - started >= max_seconds:
+                print(f"stopped: max_seconds={max_seconds} reached after {done} chunks", flush=True)
+                break
             row = runner.run(s, m) if runner else run_chunk_cli(n, threads, expanded_n, s, m, mode)
             done += 1
             total += int(row["count"])
@@ -270,7 +276,7 @@ def sweep(n: int = 8, threads: int = 16, expanded_n: int = 36,
                   f"wall_s={row['wall_s']:.2f} elapsed_s={time.perf_counter() - started:.1f}",
                   flush=True)
     summary = {
-        "chunks": len(inputs),
+        "chunks": done,
         "chunk_size": chunk_size,
         "start_case": start_case,
         "total_cases": total_cases,
@@ -313,6 +319,8 @@ def main(argv=None):
     s.add_argument("--cli", action="store_true", help="run each chunk through bin/sym_fold")
     s.add_argument("--cost-depth", type=int, default=0,
                    help="> 0: cost-weighted chunks (--chunk-count of them) scored this deep")
+    s.add_argument("--max-seconds", type=float, default=0.0,
+                   help="> 0: start no new chunk after this much wall time")
     v = sub.add_parser("validate")
     v.add_argument("--out", required=True)
     v.add_argument("--total-cases", type=int, default=TOTAL_8X8_DEPTH36_CASES)
@@ -329,7 +337,8 @@ def main(argv=None):
                                           a.start_case, a.total_cases, mode=a.mode)
             chunk_count = 0
         sweep(a.n, a.threads, a.expanded_n, a.total_cases, a.chunk_size, a.start_case,
-              chunk_count, a.out, a.resume_existing, a.mode, not a.cli, chunk_plan)
+              chunk_count, a.out, a.resume_existing, a.mode, not a.cli, chunk_plan,
+              a.max_seconds)
     else:
         validate(a.out, a.total_cases, a.chunk_size, a.expected)
 

@@ -552,6 +552,32 @@ std::atomic<uint32_t> g_inject{0};
 
 __global__ void phantom_ticket_kernel(QueueHeader *hdr) { hdr->spawn_tail = 1; }
 
+// Launch size of a persistent launch over `units` initial units searched
+// `levels` levels deep: the whole resident grid, or -- for a small job, whose
+// units are shallow (at most 10 levels to go, so none of them is heavy) --
+// about one warp per four units, with a split ring of at most two cells per
+// launched lane (at least 1024).  A tiny map then costs one small launch and
+// a short ring reset instead of thousands of warps that start, find nothing
+// and leave, and a 512 KB ring initialisation.  Deep units always get the
+// whole grid: a single deep unit can hold most of the work.
+struct LaunchShape {
+    unsigned blocks;
+    uint64_t ring;
+};
+
+LaunchShape persistent_shape(int sms, int bpsm, int tpb, uint64_t units, int levels,
+                             uint64_t ring_knob) {
+    const uint64_t full = uint64_t(sms) * uint64_t(bpsm);
+    if (levels > 10) return LaunchShape{unsigned(full), ring_knob};
+    const uint64_t warps = (units + 3) / 4;
+    const uint64_t per_block = uint64_t(tpb / 32);
+    uint64_t blocks = (warps + per_block - 1) / per_block;
+    blocks = blocks < 1 ? 1 : (blocks > full ? full : blocks);
+    uint64_t ring = 1024;
+    while (ring < 2 * blocks * uint64_t(tpb) && ring < ring_knob) ring <<= 1;
+    return LaunchShape{unsigned(blocks), ring < ring_knob ? ring : ring_knob};
+}
+
 cudaError_t reset_queue(const Queue &Q, cudaStream_t stream) {
     cudaError_t e = cudaMemsetAsync(Q.hdr, 0, 256, stream);
     if (e != cudaSuccess) return e;
@@ -626,11 +652,8 @@ cudaError_t launch_sym_batched(const uint8_t *d_edges, int start_i, int stop_i,
                                const uint8_t *d_cycles, uint64_t num, uint64_t *d_counts,
                                uint64_t *d_nodes, void *d_workspace, const BatchKnobs &knobs,
                                cudaStream_t stream) {
-    Queue Q = carve_queue(d_workspace, knobs.queue_capacity);
-    cudaError_t e = reset_queue(Q, stream);
-    if (e != cudaSuccess) return e;
-    if (num == 0) return cudaSuccess;
-    e = cudaMemsetAsync(d_counts, 0, num * sizeof(uint64_t), stream);
+    if (num == 0) return reset_queue(carve_queue(d_workspace, knobs.queue_capacity), stream);
+    cudaError_t e = cudaMemsetAsync(d_counts, 0, num * sizeof(uint64_t), stream);
     if (e != cudaSuccess) return e;
     const int sms = device_sm_count();
     const SymSource src{d_cycles, start_i, stop_i - 1};
@@ -644,7 +667,12 @@ cudaError_t launch_sym_batched(const uint8_t *d_edges, int start_i, int stop_i,
         const size_t smem = tables + Carve<TPB, 16, LV>::kThreadBytes;                           \
         e = prepare(sym_batched_kernel<TPB, LV>, smem, TPB, knobs.blocks_per_sm, bpsm);          \
         if (e != cudaSuccess) return e;                                                          \
-        sym_batched_kernel<TPB, LV><<<unsigned(sms * bpsm), TPB, smem, stream>>>(                \
+        const LaunchShape shape =                                                                \
+            persistent_shape(sms, bpsm, TPB, num, stop_i - start_i, knobs.queue_capacity);       \
+        const Queue Q = carve_queue(d_workspace, shape.ring);                                    \
+        e = reset_queue(Q, stream);                                                              \
+        if (e != cudaSuccess) return e;                                                          \
+        sym_batched_kernel<TPB, LV><<<shape.blocks, TPB, smem, stream>>>(                        \
             d_edges, src, num, counts, nodes, Q, knobs.node_budget, knobs.wait_limit);          \
     } while (0)
     if (knobs.block_threads == 256) {
@@ -671,12 +699,9 @@ cudaError_t launch_lunnon_batched(const uint8_t *d_meta, uint32_t meta_bytes, ui
                                   const uint32_t *d_state_owner, uint64_t num, uint64_t *d_counts,
                                   uint64_t *d_nodes, void *d_workspace, const BatchKnobs &knobs,
                                   cudaStream_t stream) {
-    Queue Q = carve_queue(d_workspace, knobs.queue_capacity);
-    cudaError_t e = reset_queue(Q, stream);
+    cudaError_t e = cudaMemsetAsync(d_counts, 0, size_t(num_inst) * sizeof(uint64_t), stream);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(d_counts, 0, size_t(num_inst) * sizeof(uint64_t), stream);
-    if (e != cudaSuccess) return e;
-    if (num == 0) return cudaSuccess;
+    if (num == 0) return reset_queue(carve_queue(d_workspace, knobs.queue_capacity), stream);
     const int sms = device_sm_count();
     const uint32_t mb = (meta_bytes + 15) / 16 * 16;
     const LunnonSource src{d_states, d_state_owner, nullptr, lunnon_state_stride(64)};
@@ -689,7 +714,12 @@ cudaError_t launch_lunnon_batched(const uint8_t *d_meta, uint32_t meta_bytes, ui
         const size_t smem = mb + Carve<TPB, 17, LV>::kThreadBytes;                               \
         e = prepare(lunnon_batched_kernel<TPB, LV>, smem, TPB, knobs.blocks_per_sm, bpsm);       \
         if (e != cudaSuccess) return e;                                                          \
-        lunnon_batched_kernel<TPB, LV><<<unsigned(sms * bpsm), TPB, smem, stream>>>(             \
+        const LaunchShape shape =                                                                \
+            persistent_shape(sms, bpsm, TPB, num, max_levels, knobs.queue_capacity);             \
+        const Queue Q = carve_queue(d_workspace, shape.ring);                                    \
+        e = reset_queue(Q, stream);                                                              \
+        if (e != cudaSuccess) return e;                                                          \
+        lunnon_batched_kernel<TPB, LV><<<shape.blocks, TPB, smem, stream>>>(                     \
             d_meta, mb, inst_offset, src, num, counts, nodes, Q, knobs.node_budget,             \
             knobs.wait_limit);                                                                   \
     } while (0)
