@@ -435,20 +435,8 @@ __device__ __forceinline__ void stage_sym_tables(uint8_t *smem, const uint8_t *_
 // one table byte and one list byte -- the compare-and-select of get_good's
 // `edge[j] < i` test is gone from the walk, which is bound by the integer
 // (ALU) pipe.  128 bytes per level: 3.2 KB for the 7x7 search from 24 cells.
-// Per searched level also a 32-byte record of the walk's start: the
-// admissible-position mask before any page (positions < i), the start bit of
-// each chain and the chains' start cells, so a node's walk begins with three
-// loads instead of unpacking the page table and shifting.
-struct SymLevel {
-    uint64_t low;   // positions 0 .. i-1
-    uint64_t bit_a; // 1 << start cell of chain A (0: no page, the walk is skipped)
-    uint64_t bit_b; // 1 << start cell of chain B (a copy of A with one page)
-    uint8_t o_a, o_b, pages, pad[5];
-};
-static_assert(sizeof(SymLevel) == 32, "sym level record");
-
 __host__ __device__ constexpr size_t sym_hop_bytes(int levels) {
-    return size_t(levels > 0 ? levels : 0) * (128 + sizeof(SymLevel));
+    return size_t(levels > 0 ? levels : 0) * 128;
 }
 
 template <int TPB>
@@ -463,39 +451,26 @@ __device__ __forceinline__ void stage_sym_hops(uint8_t *hop, const uint8_t *tabl
         const int p = tables[(q & 0xC0) + j];
         hop[k] = uint8_t(c != 0 && p < i ? p : j);
     }
-    SymLevel *rec = reinterpret_cast<SymLevel *>(hop + levels * 128);
-    for (int k = threadIdx.x; k < levels; k += TPB) {
-        const int i = first + k;
-        const int c = count[i];
-        const uint32_t q = pages[i];
-        const uint32_t qb = c > 1 ? (q >> 8) : q;
-        SymLevel r{};
-        r.low = low_bits(i);
-        r.o_a = uint8_t(q & 63);
-        r.o_b = uint8_t(qb & 63);
-        r.pages = uint8_t(c);
-        r.bit_a = c ? 1ULL << r.o_a : 0;
-        r.bit_b = c ? 1ULL << r.o_b : 0;
-        rec[k] = r;
-    }
 }
 
-// SymRules with the precomputed hop rows and level records (levels
-// first .. first + levels - 1).
+// SymRules with the precomputed hop rows (levels first .. first + levels - 1).
 struct SymHopRules {
     const uint8_t *hop;
-    const SymLevel *level;
+    const uint32_t *pages;
+    const uint8_t *count;
     int first;
     template <class List>
     __device__ __forceinline__ uint64_t gaps(const List &L, int i,
                                              unsigned long long &nodes) const {
         ++nodes;
-        const SymLevel &r = level[i - first];
-        if (!r.pages) return r.low;
-        const int oA = r.o_a, oB = r.o_b;
+        const uint32_t q = pages[i];
+        const int c = count[i];
+        if (c == 0) return low_bits(i);
+        const uint32_t qb = c > 1 ? (q >> 8) : q;
+        const int oA = q & 63, oB = qb & 63;
         const uint8_t *hA = hop + (i - first) * 128;
         const uint8_t *hB = hA + 64;
-        uint64_t aA = r.bit_a, aB = r.bit_b;
+        uint64_t aA = 1ULL << oA, aB = 1ULL << oB;
         int jA = L.get(oA), jB = L.get(oB);
         bool dA = jA == oA, dB = jB == oB;
         while (!(dA && dB)) {
@@ -508,16 +483,9 @@ struct SymHopRules {
             dA |= jA == oA;
             dB |= jB == oB;
         }
-        return r.low & aA & aB;
+        return low_bits(i) & aA & aB;
     }
 };
-
-// The rules over tables staged by stage_sym_hop_rules.
-__device__ __forceinline__ SymHopRules sym_hop_rules(const uint8_t *smem, int first, int levels) {
-    const uint8_t *hop = smem + 9 * kSymCells;
-    return SymHopRules{hop, reinterpret_cast<const SymLevel *>(hop + size_t(levels > 0 ? levels : 0) * 128),
-                       first};
-}
 
 // Shared-memory size of the sym tables plus the hop rows of `levels` levels.
 __host__ __device__ constexpr size_t sym_tables_bytes(int levels) {
@@ -534,7 +502,8 @@ __device__ __forceinline__ SymHopRules stage_sym_hop_rules(uint8_t *smem,
     __syncthreads();
     stage_sym_hops<TPB>(smem + 9 * kSymCells, smem, first, levels);
     __syncthreads();
-    return sym_hop_rules(smem, first, levels);
+    return SymHopRules{smem + 9 * kSymCells, reinterpret_cast<const uint32_t *>(smem + 4 * kSymCells),
+                       smem + 8 * kSymCells, first};
 }
 
 __device__ __forceinline__ SymRules sym_rules(const uint8_t *smem) {

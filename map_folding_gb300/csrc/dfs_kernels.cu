@@ -161,7 +161,9 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
     uint32_t idle_rounds = 0, round = 0;
     int reported_idle = 0;  // lane 0: idle lanes this warp last reported
     bool ring_hint = false;  // warp-uniform: the split ring probably has items
-    const SymHopRules srules = sym_hop_rules(s_tables, sym.start_i, sym.last - sym.start_i + 1);
+    const SymHopRules srules{s_tables + 9 * kSymCells,
+                             reinterpret_cast<const uint32_t *>(s_tables + 4 * kSymCells),
+                             s_tables + 8 * kSymCells, sym.start_i};
     LunnonRules lrules{s_tables, 0, 0};
 
     // Prefetch state: 0 = no initial unit left for this lane, 1 = index
