@@ -155,6 +155,8 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
     bool busy = false, fresh = false;
+    bool walking = false;  // sym: a resumable walk is under way
+    SymHopRules::Walk walk{};
     int lvl = 0, root = 0, last = 0, eval = 0;
     uint32_t owner = 0;
     unsigned long long leaves = 0, nodes = 0, finished = 0, started = 0;
@@ -230,6 +232,7 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
             lvl = root;
             S.set(root, uint64_t(w[18]) | (uint64_t(w[19]) << 32));
             eval = advance(L, S, lvl, root);  // an item's mask is never empty
+            walking = false;
             fresh = false;
             busy = eval >= 0;
         }
@@ -304,6 +307,7 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
                 } else {
                     busy = true;
                     fresh = true;
+                    walking = false;
                     lvl = root;
                     eval = root;
                 }
@@ -356,16 +360,32 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
         }
         idle_rounds = 0;
         nap = 256;
-        // One evaluation per busy lane.
+        // One round of evaluation per busy lane: sym walks take at most
+        // kWalkCap steps and go on in the next round if unfinished; a Lunnon
+        // node is evaluated whole.
         if (busy) {
-            uint64_t g;
-            if (kSym) g = srules.gaps(L, eval, nodes);
-            else g = lrules.gaps(L, eval, nodes);
-            eval = apply_advance(L, S, lvl, eval, root, last, fresh, g, leaves);
-            fresh = false;
-            if (eval < 0) {
-                flush();
-                busy = false;
+            uint64_t g = 0;
+            bool evaluated = true;
+            if (kSym) {
+                if (!walking) {
+                    srules.begin(L, eval, nodes, walk);
+                    walking = true;
+                }
+                evaluated = srules.run(L, walk, kWalkCap);
+                if (evaluated) {
+                    walking = false;
+                    g = srules.result(walk);
+                }
+            } else {
+                g = lrules.gaps(L, eval, nodes);
+            }
+            if (evaluated) {
+                eval = apply_advance(L, S, lvl, eval, root, last, fresh, g, leaves);
+                fresh = false;
+                if (eval < 0) {
+                    flush();
+                    busy = false;
+                }
             }
         }
         if (!bookkeeping) continue;
