@@ -161,9 +161,14 @@ typedef struct {
     uint64_t seed_count;  /* MF_SEED_COUNT: representatives kept (0 = the rest) */
 } mf_sym_plan_options;
 
-/* mf_sym_plan_create with sym_fold9's setup options; n may be 9.  Cases are
- * expanded on the host to at most 64 cells (expanded_n <= 64), and counting
- * past cell 63 runs on the 128-bit kernel.  A seed slice keeps centre
+/* mf_sym_plan_create with sym_fold9's setup options; n may be 9, and
+ * expanded_n up to n*n as in sym_fold9 (sym_fold9.cpp:1094-1099).  Counting
+ * past cell 63 runs on the 128-bit kernel.  Cases expanded past 64 cells are
+ * records of 96 bytes (mf_sym_plan_case_bytes) and are streamed: there is no
+ * case-count index (counting the cases below every prefix would be a large
+ * part of the 9x9 search), a chunk is reached by walking the cases in
+ * emission order from the first -- sym_fold9's stream mode -- the plan's
+ * total is reported as 0, and max_cases must be given.  A seed slice keeps centre
  * representatives [seed_start, seed_start + seed_count) and numbers cases
  * within the slice, as sym_fold9 does.
  * Replaces: sym_fold9.cpp:969-981 (choose_center_size), :1037-1124 (setup;
@@ -178,8 +183,13 @@ int32_t mf_sym_plan_info(const mf_sym_plan *plan, int32_t *n, int32_t *start_i,
                          uint64_t *center_cases, uint64_t *reduced_cases,
                          uint64_t *total_cases);
 
+/* Bytes per case record of a plan: 64, or 96 for cases expanded past 64
+ * cells.  No reference counterpart (the reference keeps cases in memory). */
+uint32_t mf_sym_plan_case_bytes(const mf_sym_plan *plan);
+
 /* Cases [start_case, start_case + max_cases) of the deterministic emission
- * order (max_cases == 0: to the end), each as a 64-byte cycle plus its orbit
+ * order (max_cases == 0: to the end), each as a cycle record of
+ * mf_sym_plan_case_bytes bytes (successor cell of each cell) plus its orbit
  * multiplier.  Seeks through a per-representative case-count index instead
  * of walking every earlier case.  *count_out gets the number selected.
  * Replaces: sym_fold.cpp:491-527 (recurse_stream_cases), :731-745. */

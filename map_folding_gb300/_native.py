@@ -133,6 +133,7 @@ SIGNATURES = {
     "mf_sym_plan_destroy": ([_p], None),
     "mf_sym_plan_info": ([_p, _p, _p, _p, _p, _p], _i32),
     "mf_sym_cases": ([_p, _u64, _u64, _p, _p, _u64, _pu64], _i32),
+    "mf_sym_plan_case_bytes": ([_p], _u32),
     "mf_sym_count_cases": ([_i32, _i32, _i32, _p, _u64, _p, _p, _p], _i32),
     "mf_sym_workspace_bytes": ([_p], _u64),
     "mf_sym_count_cases_batched": ([_i32, _i32, _i32, _p, _u64, _p, _p, _p, _u64, _p, _p], _i32),

@@ -265,12 +265,22 @@ class SymPlan:
         except Exception:
             pass
 
+    @property
+    def case_bytes(self) -> int:
+        """Bytes per case record: 64, or 96 for cases expanded past 64 cells."""
+        return int(_native.load().mf_sym_plan_case_bytes(self._h))
+
     def cases(self, start_case: int = 0, max_cases: int = 0):
-        """(cycles [k, 64] uint8, multipliers [k] uint64)."""
+        """(cycles [k, case_bytes] uint8, multipliers [k] uint64).  Plans
+        whose cases go past 64 cells are streamed (no total): max_cases is
+        then required."""
         lib = _native.load()
-        avail = max(self.total_cases - start_case, 0)
-        want = avail if max_cases == 0 else min(avail, max_cases)
-        cyc = np.zeros((max(want, 1), 64), np.uint8)
+        if self.case_bytes > 64:
+            want = max_cases
+        else:
+            avail = max(self.total_cases - start_case, 0)
+            want = avail if max_cases == 0 else min(avail, max_cases)
+        cyc = np.zeros((max(want, 1), self.case_bytes), np.uint8)
         mult = np.zeros(max(want, 1), np.uint64)
         out = ctypes.c_uint64()
         check(lib.mf_sym_cases(self._h, start_case, max_cases, cyc.ctypes.data, mult.ctypes.data,

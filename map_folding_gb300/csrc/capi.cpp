@@ -781,7 +781,7 @@ int32_t mf_sym_plan_create_ex(int32_t n, const mf_sym_plan_options *opts, mf_sym
         set_error("%s", why.c_str());
         return rc;
     }
-    if (plan->p.mid_first.empty()) {
+    if (plan->p.mid_first.empty() && !plan->p.streamed) {
         rc = complete_index(plan->p);
         if (rc) return rc;
     }
@@ -801,7 +801,7 @@ int build_full_sym_plan(int n, int expanded_n, SymPlan &plan) {
         set_error("%s", why.c_str());
         return rc;
     }
-    if (plan.mid_first.empty()) return complete_index(plan);
+    if (plan.mid_first.empty() && !plan.streamed) return complete_index(plan);
     return MF_OK;
 }
 }  // namespace mf
@@ -830,9 +830,17 @@ int32_t mf_sym_cases(const mf_sym_plan *plan, uint64_t start_case, uint64_t max_
         set_error("plan and count_out are required");
         return MF_ERR_ARG;
     }
+    if (plan->p.streamed && !max_cases) {
+        set_error("cases expanded past 64 cells are streamed: max_cases must be given");
+        return MF_ERR_ARG;
+    }
     *count_out = sym_select_cases(plan->p, start_case, max_cases, cycles, mults,
                                   (cycles || mults) ? cap : 0);
     return MF_OK;
+}
+
+uint32_t mf_sym_plan_case_bytes(const mf_sym_plan *plan) {
+    return plan ? plan->p.case_bytes : 0;
 }
 
 static int check_sym_range(int32_t n, int32_t start_i, int32_t stop_i) {
@@ -917,9 +925,9 @@ namespace {
 // 1: batched.  Per-case counts land in h_counts.  Returns mf_status.
 int count_cases_host(int n, int start_i, int stop_i, const uint8_t *h_cycles, uint64_t num,
                      int mode, const mf_batch_config *cfg, uint64_t *h_counts, mf_run_stats *st,
-                     QueueHeader *hdr_out) {
+                     QueueHeader *hdr_out, uint32_t record_bytes = kSymCells) {
     std::lock_guard<std::recursive_mutex> scratch_lock(g_scratch_mu);
-    const size_t in_bytes = num * kSymCells;
+    const size_t in_bytes = num * record_bytes;
     const BatchKnobs knobs = resolve_knobs(cfg);
     // Searches past cell 63 run on the 128-bit kernel (batched only);
     // stack_mode 2 selects it for any board.
@@ -945,7 +953,8 @@ int count_cases_host(int n, int start_i, int stop_i, const uint8_t *h_cycles, ui
     cudaEventRecord(th.b, s);
     cudaEventRecord(tk.a, s);
     if (wide)
-        MF_TRY_CUDA(launch_sym_wide(edges, start_i, stop_i, d_cycles, num, d_counts, d_counts + num,
+        MF_TRY_CUDA(launch_sym_wide(edges, start_i, stop_i, d_cycles, record_bytes, num, d_counts,
+                                    d_counts + num,
                                     d_work, knobs, s));
     else if (mode == 1)
         MF_TRY_CUDA(launch_sym_batched(edges, start_i, stop_i, d_cycles, num, d_counts,
@@ -1092,7 +1101,17 @@ int32_t mf_sym_plan_solve(const mf_sym_plan *plan, uint64_t max_cases, uint64_t 
     const SymPlan &p = plan->p;
     uint64_t want = p.total_cases > start_case ? p.total_cases - start_case : 0;
     if (max_cases && max_cases < want) want = max_cases;
-    auto *cycles = static_cast<uint8_t *>(scratch(kHostUnits, std::max<uint64_t>(want, 1) * kSymCells, true));
+    if (p.streamed) {
+        // No index past 64 cells: the chunk is walked to from the first case
+        // (as sym_fold9's stream mode does), so its size must be given.
+        if (!max_cases) {
+            set_error("cases expanded past 64 cells are streamed: max_cases must be given");
+            return MF_ERR_ARG;
+        }
+        want = max_cases;
+    }
+    auto *cycles = static_cast<uint8_t *>(
+        scratch(kHostUnits, std::max<uint64_t>(want, 1) * p.case_bytes, true));
     std::vector<uint64_t> mults(std::max<uint64_t>(want, 1));
     if (!cycles) return MF_ERR_CUDA;
     const uint64_t got = sym_select_cases(p, start_case, want, cycles, mults.data(), want);
@@ -1100,7 +1119,7 @@ int32_t mf_sym_plan_solve(const mf_sym_plan *plan, uint64_t max_cases, uint64_t 
     std::vector<uint64_t> counts(got + 1);
     if (got) {
         rc = count_cases_host(p.n, p.start_i, p.n * p.n, cycles, got, mode, cfg, counts.data(), st,
-                              nullptr);
+                              nullptr, p.case_bytes);
         if (rc) return rc;
     }
     u128 sum = 0;

@@ -319,13 +319,24 @@ int main(int argc, char **argv) {
         // exactly (the answer is linear in the cases).
         unsigned long long planned = total > start_case ? total - start_case : 0;
         if (max_cases && max_cases < planned) planned = max_cases;
+        // Cases past 64 cells have no index: the chunk is walked to from the
+        // first case, so it runs as one piece (each piece would walk again).
+        const bool deep = mf_sym_plan_case_bytes(plan) > 64;
+        if (deep) {
+            if (!max_cases) {
+                std::fprintf(stderr, "error: cases expanded past 64 cells are streamed: give max_cases\n");
+                mf_sym_plan_destroy(plan);
+                return 2;
+            }
+            planned = max_cases;
+        }
         int rc = MF_OK;
         {
             Progress prog;
             ProgressPrinter printer(prog, stream, planned);
             unsigned __int128 sum = 0;
             unsigned long long done = 0;
-            unsigned long long piece = std::min<unsigned long long>(planned, 4096);
+            unsigned long long piece = deep ? planned : std::min<unsigned long long>(planned, 4096);
             while (done < planned) {
                 prog.selected = done + piece;
                 if (done + piece == planned) prog.producer_done = 1;
@@ -340,6 +351,7 @@ int main(int argc, char **argv) {
                 st.nodes += ps.nodes;
                 st.splits += ps.splits;
                 done += piece;
+                if (deep) done = planned;  // a short final chunk ends the stream
                 prog.completed = done;
                 const double el = since(ts);
                 const double rate = el > 0.0 ? double(piece) / el : 1e9;

@@ -17,6 +17,10 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kLocalLevels = 66;    // local-memory stack: levels 0..65
 constexpr int kMinSplitHeight = 4;  // never hand out subtrees shallower than this
+// Steps a resumable walk may take per lockstep round (measured on the 7x7
+// cases: 6 steps gave 8 % more nodes per second than uncapped walks, 8 steps
+// 6.5 %, 10 steps 2 %).
+constexpr int kWalkCap = 6;
 
 __device__ __forceinline__ uint64_t low_bits(int k) {
     return k >= 64 ? ~0ULL : ((1ULL << k) - 1ULL);
@@ -168,41 +172,87 @@ struct LunnonRules {
     const uint8_t *table;  // [dim][n+1][n+1]
     int n;
     int dim;
+
+    // A resumable walk (see SymHopRules): the constrained dimensions are
+    // walked two at a time; run() takes at most `cap` steps in all.
+    struct Walk {
+        const uint8_t *rA, *rB;
+        uint64_t mask, wA, wB;
+        int mA, mB, l, d, bound;
+        bool dA, dB, active;
+    };
+
+    // The next pair of constrained dimensions from w.d on (one of them twice
+    // if only one is left); false when there is none.
+    __device__ __forceinline__ bool next_pair(Walk &w) const {
+        const int wd = n + 1;
+        const uint8_t *rA = nullptr, *rB = nullptr;
+        for (; w.d < dim && !rB; ++w.d) {
+            const uint8_t *row = table + (w.d * wd + w.l) * wd;
+            if (row[w.l] == w.l) continue;  // unconstrained dimension
+            if (!rA) rA = row;
+            else rB = row;
+        }
+        if (!rA) return false;
+        if (!rB) rB = rA;
+        ++w.bound;
+        w.rA = rA;
+        w.rB = rB;
+        w.mA = rA[w.l];
+        w.mB = rB[w.l];
+        w.wA = w.wB = 0;
+        w.dA = w.dB = false;
+        return true;
+    }
+
+    template <class List>
+    __device__ __forceinline__ void begin(const List &L, int l, unsigned long long &,
+                                          Walk &w) const {
+        w.l = l;
+        w.mask = low_bits(l);
+        w.bound = 0;
+        w.d = 0;
+        L.put(l, l);
+        w.active = next_pair(w);
+    }
+
+    template <class List>
+    __device__ __forceinline__ bool run(const List &L, Walk &w, int cap) const {
+        for (int k = 0; k < cap && w.active; ++k) {
+            if (w.dA && w.dB) {  // this pair is done: fold it in, go on to the next
+                w.mask &= w.wA & w.wB;
+                w.active = w.mask && next_pair(w);
+                if (!w.active) break;
+            }
+            w.wA |= bit64(w.mA);
+            w.wB |= bit64(w.mB);
+            w.dA |= w.mA == w.l;
+            w.dB |= w.mB == w.l;
+            w.mA = w.rA[L.get(w.mA)];
+            w.mB = w.rB[L.get(w.mB)];
+        }
+        if (w.active && w.dA && w.dB) {  // the last pair finished on the last step
+            w.mask &= w.wA & w.wB;
+            w.active = w.mask && next_pair(w);
+        }
+        return !w.active;
+    }
+
+    // The node's positions; counts the insertions the reference would make.
+    __device__ __forceinline__ uint64_t result(const Walk &w, unsigned long long &nodes) const {
+        uint64_t mask = w.bound ? w.mask : low_bits(w.l);
+        nodes += __popcll(mask);
+        if (w.l >= 2) mask &= ~1ULL;
+        return mask;
+    }
+
     template <class List>
     __device__ __forceinline__ uint64_t gaps(const List &L, int l,
                                              unsigned long long &nodes) const {
-        const int w = n + 1;
-        uint64_t mask = low_bits(l);
-        int bound = 0, d = 0;
-        L.put(l, l);
-        while (mask) {
-            const uint8_t *rA = nullptr, *rB = nullptr;
-            for (; d < dim && !rB; ++d) {
-                const uint8_t *row = table + (d * w + l) * w;
-                if (row[l] == l) continue;  // unconstrained dimension
-                if (!rA) rA = row;
-                else rB = row;
-            }
-            if (!rA) break;
-            if (!rB) rB = rA;
-            ++bound;
-            int mA = rA[l], mB = rB[l];
-            uint64_t wA = 0, wB = 0;
-            bool dA = false, dB = false;
-            while (!(dA && dB)) {
-                wA |= bit64(mA);
-                wB |= bit64(mB);
-                dA |= mA == l;
-                dB |= mB == l;
-                mA = rA[L.get(mA)];
-                mB = rB[L.get(mB)];
-            }
-            mask &= wA & wB;
-        }
-        if (!bound) mask = low_bits(l);
-        nodes += __popcll(mask);
-        if (l >= 2) mask &= ~1ULL;
-        return mask;
+        Walk w;
+        begin(L, l, nodes, w);
+        run(L, w, 1 << 30);
+        return result(w, nodes);
     }
 };
 
@@ -385,7 +435,8 @@ __device__ __forceinline__ void init_stack(LocalStack &S, uint8_t *, size_t) {
 }
 
 // Run one loaded unit per lane to completion in lockstep rounds (no refill):
-// the plain one-thread-per-unit kernels.
+// the plain one-thread-per-unit kernels.  Walks are resumable and take at
+// most kWalkCap steps per round.
 template <class Rules, class Stk, int TPB>
 __device__ __forceinline__ void run_units(const Rules &R, const List<TPB> &L, Stk &S, bool busy,
                                           int root, int last, unsigned long long &leaves,
@@ -396,12 +447,21 @@ __device__ __forceinline__ void run_units(const Rules &R, const List<TPB> &L, St
         leaves += 1;
         busy = false;
     }
+    bool walking = false;
+    typename Rules::Walk w;
     while (__any_sync(kFull, busy)) {
         if (busy) {
-            const uint64_t g = R.gaps(L, eval, nodes);
-            eval = apply_advance(L, S, lvl, eval, root, last, fresh, g, leaves);
-            fresh = false;
-            busy = eval >= 0;
+            if (!walking) {
+                R.begin(L, eval, nodes, w);
+                walking = true;
+            }
+            if (R.run(L, w, kWalkCap)) {
+                walking = false;
+                const uint64_t g = R.result(w, nodes);
+                eval = apply_advance(L, S, lvl, eval, root, last, fresh, g, leaves);
+                fresh = false;
+                busy = eval >= 0;
+            }
         }
     }
 }
@@ -514,7 +574,7 @@ struct SymHopRules {
         return w.dA && w.dB;
     }
 
-    __device__ __forceinline__ uint64_t result(const Walk &w) const {
+    __device__ __forceinline__ uint64_t result(const Walk &w, unsigned long long &) const {
         return low_bits(w.i) & w.aA & w.aB;
     }
 
@@ -524,42 +584,11 @@ struct SymHopRules {
         Walk w;
         begin(L, i, nodes, w);
         run(L, w, 1 << 30);
-        return result(w);
+        return result(w, nodes);
     }
 };
 
-// Steps a resumable walk may take per lockstep round (measured on the 7x7
-// cases: 6 steps gave 8 % more nodes per second than uncapped walks, 8 steps
-// 6.5 %, 10 steps 2 %).
-constexpr int kWalkCap = 6;
 
-// run_units with resumable walks capped at kWalkCap steps per round.
-template <class Stk, int TPB>
-__device__ __forceinline__ void run_units(const SymHopRules &R, const List<TPB> &L, Stk &S,
-                                          bool busy, int root, int last,
-                                          unsigned long long &leaves, unsigned long long &nodes) {
-    int lvl = root, eval = root;
-    bool fresh = true, walking = false;
-    SymHopRules::Walk w;
-    if (busy && root > last) {  // nothing left to place: one completion
-        leaves += 1;
-        busy = false;
-    }
-    while (__any_sync(kFull, busy)) {
-        if (busy) {
-            if (!walking) {
-                R.begin(L, eval, nodes, w);
-                walking = true;
-            }
-            if (R.run(L, w, kWalkCap)) {
-                walking = false;
-                eval = apply_advance(L, S, lvl, eval, root, last, fresh, R.result(w), leaves);
-                fresh = false;
-                busy = eval >= 0;
-            }
-        }
-    }
-}
 
 // Shared-memory size of the sym tables plus the hop rows of `levels` levels.
 __host__ __device__ constexpr size_t sym_tables_bytes(int levels) {

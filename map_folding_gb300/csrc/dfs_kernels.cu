@@ -155,8 +155,9 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
     bool busy = false, fresh = false;
-    bool walking = false;  // sym: a resumable walk is under way
-    SymHopRules::Walk walk{};
+    bool walking = false;  // a resumable walk is under way
+    SymHopRules::Walk swalk{};
+    LunnonRules::Walk lwalk{};
     int lvl = 0, root = 0, last = 0, eval = 0;
     uint32_t owner = 0;
     unsigned long long leaves = 0, nodes = 0, finished = 0, started = 0;
@@ -360,26 +361,28 @@ __device__ __forceinline__ void persistent_loop(const uint8_t *s_tables,
         }
         idle_rounds = 0;
         nap = 256;
-        // One round of evaluation per busy lane: sym walks take at most
-        // kWalkCap steps and go on in the next round if unfinished; a Lunnon
-        // node is evaluated whole.
+        // One round of evaluation per busy lane: a walk takes at most
+        // kWalkCap steps and goes on in the next round if unfinished.
         if (busy) {
             uint64_t g = 0;
-            bool evaluated = true;
+            bool evaluated;
             if (kSym) {
                 if (!walking) {
-                    srules.begin(L, eval, nodes, walk);
+                    srules.begin(L, eval, nodes, swalk);
                     walking = true;
                 }
-                evaluated = srules.run(L, walk, kWalkCap);
-                if (evaluated) {
-                    walking = false;
-                    g = srules.result(walk);
-                }
+                evaluated = srules.run(L, swalk, kWalkCap);
+                if (evaluated) g = srules.result(swalk, nodes);
             } else {
-                g = lrules.gaps(L, eval, nodes);
+                if (!walking) {
+                    lrules.begin(L, eval, nodes, lwalk);
+                    walking = true;
+                }
+                evaluated = lrules.run(L, lwalk, kWalkCap);
+                if (evaluated) g = lrules.result(lwalk, nodes);
             }
             if (evaluated) {
+                walking = false;
                 eval = apply_advance(L, S, lvl, eval, root, last, fresh, g, leaves);
                 fresh = false;
                 if (eval < 0) {

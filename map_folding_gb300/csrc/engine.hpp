@@ -65,6 +65,8 @@ void sym_edges(int n, uint8_t *out /* 4*64 */);
 // The same pages with `stride` cells each (cells >= stride left out).
 void sym_edges_stride(int n, uint8_t *out, int stride);
 uint64_t sym_good_host(const uint8_t *cycle, int i, const uint8_t *edges);
+void sym_good_host_wide(const uint8_t *cycle, int i, const uint8_t *wide_edges, uint64_t &lo,
+                        uint64_t &hi);
 
 struct SymPlan {
     int n = 0;
@@ -92,6 +94,14 @@ struct SymPlan {
     // indices refer to that order, as in the reference's materialized mode.
     std::vector<uint8_t> sorted_cycles;
     std::vector<uint64_t> sorted_mult;
+    // Cases expanded past 64 cells (9x9, MF_EXPANDED_N up to 81): records of
+    // kWideCells bytes, and no case-count index -- counting every case below
+    // each prefix would be a large part of the 9x9 search itself -- so a chunk
+    // is reached by walking the cases in emission order from the first, as
+    // experiments/9x9/sym_fold9.cpp does in its stream mode (total_cases is
+    // then unknown, 0).
+    bool streamed = false;
+    uint32_t case_bytes = kSymCells;
 };
 
 // The reference's cost order (sym_fold.cpp:297-310): std::sort of the cases
@@ -116,6 +126,8 @@ int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why, int c
 // Returns false if stopped.
 template <class F>
 bool sym_expand(uint8_t *cycle, int from, int stop, const uint8_t *edges, F &&emit);
+template <class F>
+bool sym_expand_wide(uint8_t *cycle, int from, int stop, const uint8_t *wide_edges, F &&emit);
 
 // Select cases [start, start+max) into cycles/mults; returns count selected.
 uint64_t sym_select_cases(const SymPlan &plan, uint64_t start, uint64_t max_cases,
@@ -188,10 +200,12 @@ cudaError_t launch_sym_plain(const uint8_t *d_edges, int start_i, int stop_i,
                              const uint8_t *d_cycles, uint64_t num, uint64_t *d_counts,
                              uint64_t *d_nodes, cudaStream_t stream);
 // The 128-bit batched search for boards over 64 cells (wide_kernels.cu):
-// d_wide_edges holds 4 pages of kWideCells, cases are 64-byte records with
-// start_i <= 64 cells placed, stop_i <= kWideCells.
+// d_wide_edges holds 4 pages of kWideCells, cases are records of
+// record_bytes (64, or kWideCells for expansions past 64 cells) with start_i
+// <= record_bytes cells placed, stop_i <= kWideCells.
 cudaError_t launch_sym_wide(const uint8_t *d_wide_edges, int start_i, int stop_i,
-                            const uint8_t *d_cycles, uint64_t num, uint64_t *d_counts,
+                            const uint8_t *d_cycles, uint32_t record_bytes, uint64_t num,
+                            uint64_t *d_counts,
                             uint64_t *d_nodes, void *d_workspace, const BatchKnobs &knobs,
                             cudaStream_t stream);
 

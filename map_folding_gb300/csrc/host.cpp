@@ -255,6 +255,31 @@ uint64_t sym_good_host(const uint8_t *cycle, int i, const uint8_t *edges) {
     return good;
 }
 
+// sym_fold9.cpp:286-312: get_good with 128-bit masks over kWideCells cells.
+void sym_good_host_wide(const uint8_t *cycle, int i, const uint8_t *wide_edges, uint64_t &lo,
+                        uint64_t &hi) {
+    lo = i >= 64 ? ~0ULL : ((1ULL << i) - 1);
+    hi = i <= 64 ? 0 : (i >= 128 ? ~0ULL : ((1ULL << (i - 64)) - 1));
+    for (int page = 0; page < 4; ++page) {
+        const uint8_t *e = wide_edges + page * kWideCells;
+        const int other = e[i];
+        if (other >= i) continue;
+        uint64_t alo = 0, ahi = 0;
+        auto mark = [&](int x) {
+            if (x < 64) alo |= 1ULL << x;
+            else ahi |= 1ULL << (x - 64);
+        };
+        mark(other);
+        for (int j = cycle[other]; j != other; j = cycle[j]) {
+            if (e[j] < i) j = e[j];
+            mark(j);
+        }
+        lo &= alo;
+        hi &= ahi;
+        if (!lo && !hi) return;
+    }
+}
+
 namespace {
 
 constexpr int kMaxCentre = 25;  // 5 x 5 centre (experiments/9x9/sym_fold9.cpp:33)
@@ -341,9 +366,9 @@ int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why, int c
     } else {
         plan.start_i = plan.seed_i;
     }
-    if (plan.start_i > kSymCells) {
-        why = "cases are expanded on the host to at most " + std::to_string(kSymCells) + " cells";
-        return MF_ERR_ARG;
+    if (plan.start_i > kSymCells) {  // only boards over 64 cells get here (9x9)
+        plan.streamed = true;
+        plan.case_bytes = kWideCells;
     }
     plan.edges.resize(4 * kSymCells);
     sym_edges(n, plan.edges.data());  // boards over 64 cells: the 64-cell projection
@@ -458,7 +483,8 @@ int build_sym_plan(int n, int expanded_n, SymPlan &plan, std::string &why, int c
         for (uint64_t k = 0; k <= mids; ++k) plan.mid_first[k] = k;
         plan.total_cases = mids;
     }
-    // else: mid_first is filled by the index completion (needs the GPU).
+    // else: mid_first is filled by the index completion (needs the GPU),
+    // except for streamed plans, which have none.
     return MF_OK;
 }
 
@@ -491,6 +517,34 @@ uint64_t sym_select_cases(const SymPlan &plan, uint64_t start, uint64_t max_case
             if (mults) mults[k - start] = plan.sorted_mult[k];
         }
         return end - start;
+    }
+    if (plan.streamed) {
+        // Walk the cases in emission order from the first (sym_fold9's stream
+        // mode), expanding each depth-mid prefix past 64 cells with 128-bit
+        // masks; max_cases must be given (the total is unknown).
+        if (max_cases == 0) return 0;
+        uint64_t skip = start, got = 0;
+        const uint64_t mids = plan.mid_mult.size();
+        uint8_t cyc[kWideCells];
+        for (uint64_t k = 0; k < mids && got < max_cases; ++k) {
+            std::memset(cyc, 0, sizeof(cyc));
+            std::memcpy(cyc, &plan.mid_cycles[k * kSymCells], kSymCells);
+            const uint64_t mult = plan.mid_mult[k];
+            sym_expand_wide(cyc, plan.mid_i, plan.start_i, plan.wide_edges.data(),
+                            [&](const uint8_t *c) {
+                                if (skip > 0) {
+                                    --skip;
+                                    return true;
+                                }
+                                if (got < cap) {
+                                    if (cycles) std::memcpy(cycles + got * kWideCells, c, kWideCells);
+                                    if (mults) mults[got] = mult;
+                                }
+                                ++got;
+                                return got < max_cases;
+                            });
+        }
+        return got;
     }
     if (plan.mid_first.empty() || start >= plan.total_cases) return 0;
     uint64_t end = plan.total_cases;

@@ -240,7 +240,7 @@ __device__ __forceinline__ void wide_put(uint4 *slots, const Queue &Q, unsigned 
 template <int TPB, int LEVELS>
 __global__ void __launch_bounds__(TPB)
     sym_wide_kernel(const uint8_t *__restrict__ edges, int start_i, int last,
-                    const uint8_t *__restrict__ cycles, unsigned long long num,
+                    const uint8_t *__restrict__ cycles, uint32_t record_bytes, unsigned long long num,
                     unsigned long long *counts, unsigned long long *nodes_out, Queue Q,
                     uint4 *slots, uint32_t period, uint32_t wait_limit) {
     extern __shared__ __align__(16) uint8_t smem[];
@@ -342,17 +342,19 @@ __global__ void __launch_bounds__(TPB)
             if (!busy && init_left) {
                 const unsigned long long k = base + __popc(want_init & lt_mask);
                 if (k < num) {
-                    const uint4 *src = reinterpret_cast<const uint4 *>(cycles + k * kSymCells);
+                    // 64-byte records (cases of at most 64 cells) or 96-byte
+                    // ones (deeper 9x9 expansions); list words past the
+                    // record start as zeros.
+                    const uint4 *src = reinterpret_cast<const uint4 *>(cycles + k * record_bytes);
+                    const int vecs = int(record_bytes / 16);
 #pragma unroll
-                    for (int q = 0; q < kSymCells / 16; ++q) {
-                        const uint4 x = __ldg(src + q);
+                    for (int q = 0; q < kWideWords / 4; ++q) {
+                        const uint4 x = q < vecs ? __ldg(src + q) : make_uint4(0, 0, 0, 0);
                         L.set_word(4 * q, x.x);
                         L.set_word(4 * q + 1, x.y);
                         L.set_word(4 * q + 2, x.z);
                         L.set_word(4 * q + 3, x.w);
                     }
-#pragma unroll
-                    for (int q = kSymCells / 4; q < kWideWords; ++q) L.set_word(q, 0);
                     owner = uint32_t(k);
                     root = start_i;
                     ++started;
@@ -466,7 +468,7 @@ constexpr int kWideTPB = 64;
 
 template <int LEVELS>
 cudaError_t launch_wide_levels(const uint8_t *d_edges, int start_i, int last, const uint8_t *d_cycles,
-                               uint64_t num, uint64_t *d_counts, uint64_t *d_nodes, const Queue &Q,
+                               uint32_t record_bytes, uint64_t num, uint64_t *d_counts, uint64_t *d_nodes, const Queue &Q,
                                uint4 *slots, const BatchKnobs &knobs, cudaStream_t stream) {
     static std::mutex mu;
     static bool raised[16] = {};
@@ -491,7 +493,8 @@ cudaError_t launch_wide_levels(const uint8_t *d_edges, int start_i, int last, co
     if (fit < 1) return cudaErrorInvalidConfiguration;
     if (knobs.blocks_per_sm > 0 && int(knobs.blocks_per_sm) < fit) fit = int(knobs.blocks_per_sm);
     sym_wide_kernel<kWideTPB, LEVELS><<<unsigned(device_sm_count() * fit), kWideTPB, smem, stream>>>(
-        d_edges, start_i, last, d_cycles, num, reinterpret_cast<unsigned long long *>(d_counts),
+        d_edges, start_i, last, d_cycles, record_bytes, num,
+        reinterpret_cast<unsigned long long *>(d_counts),
         reinterpret_cast<unsigned long long *>(d_nodes), Q, slots, knobs.node_budget,
         knobs.wait_limit);
     return cudaGetLastError();
@@ -504,7 +507,8 @@ uint64_t wide_workspace_bytes(uint64_t capacity) {
 }
 
 cudaError_t launch_sym_wide(const uint8_t *d_wide_edges, int start_i, int stop_i,
-                            const uint8_t *d_cycles, uint64_t num, uint64_t *d_counts,
+                            const uint8_t *d_cycles, uint32_t record_bytes, uint64_t num,
+                            uint64_t *d_counts,
                             uint64_t *d_nodes, void *d_workspace, const BatchKnobs &knobs,
                             cudaStream_t stream) {
     const uint64_t cap = knobs.queue_capacity;
@@ -525,13 +529,16 @@ cudaError_t launch_sym_wide(const uint8_t *d_wide_edges, int start_i, int stop_i
     const int levels = stop_i - 1 - start_i;
     // Stored levels run up to stop_i - 2; their high words need rows up to
     // stop_i - 2 - 65 < kWideHiRows.
-    if (start_i > kSymCells || stop_i > 66 + kWideHiRows || stop_i > kWideCells)
+    if ((record_bytes != kSymCells && record_bytes != kWideCells) || start_i > int(record_bytes) ||
+        stop_i > 66 + kWideHiRows || stop_i > kWideCells)
         return cudaErrorInvalidValue;
     if (levels <= 40)
-        return launch_wide_levels<40>(d_wide_edges, start_i, stop_i - 1, d_cycles, num, d_counts,
+        return launch_wide_levels<40>(d_wide_edges, start_i, stop_i - 1, d_cycles, record_bytes, num,
+                                      d_counts,
                                       d_nodes, Q, slots, knobs, stream);
     if (levels <= 56)
-        return launch_wide_levels<56>(d_wide_edges, start_i, stop_i - 1, d_cycles, num, d_counts,
+        return launch_wide_levels<56>(d_wide_edges, start_i, stop_i - 1, d_cycles, record_bytes, num,
+                                      d_counts,
                                       d_nodes, Q, slots, knobs, stream);
     return cudaErrorInvalidValue;  // deeper searches need a deeper expansion first
 }

@@ -4,6 +4,7 @@ solvers, built from source by `make -C oracle ref` into oracle/_ref/.
     python tests/golden/make_golden.py          # needs oracle/_ref/{mf,mf_fast,sym_fold}
     python tests/golden/make_golden.py --cost   # refresh only the cost-order vectors
     python tests/golden/make_golden.py --sym9   # refresh only the sym_fold9 (9x9) vectors
+    python tests/golden/make_golden.py --sym9-deep  # add the 9x9 chunks expanded past 64 cells
     python tests/golden/make_golden.py --high-dim  # refresh only the 3- to 5-D Lunnon maps
     python tests/golden/make_golden.py --published # rewrite only the published values
     python tests/golden/make_golden.py --serving   # the serving stream's 8x8 chunks (hours, resumable)
@@ -96,6 +97,32 @@ def sym9_jobs():
         ("9x9_c5_seed1000x10_d44_20+300", [s9, 9, 8, 300, 20],
          dict(c5, MF_EXPANDED_N="44", MF_SEED_START="1000", MF_SEED_COUNT="10")),
     ]
+
+
+def sym9_deep_jobs():
+    """sym_fold9 with MF_EXPANDED_N past 64 cells (sym_fold9.cpp:1094-1099
+    allows up to n*n): streamed chunks of the 5x5-centre 9x9 cases."""
+    s9 = REF / "sym_fold9"
+    c5 = {"MF_CENTER_N": "5", "MF_CENTER_STREAM_DEDUP": "1", "MF_STREAM_CASES": "1"}
+    return [
+        ("9x9_c5_d66_first100", [s9, 9, 8, 100, 0], dict(c5, MF_EXPANDED_N="66")),
+        ("9x9_c5_d72_first100", [s9, 9, 8, 100, 0], dict(c5, MF_EXPANDED_N="72")),
+        ("9x9_c5_d66_3000+200", [s9, 9, 8, 200, 3000], dict(c5, MF_EXPANDED_N="66")),
+        ("9x9_c5_d80_first50", [s9, 9, 8, 50, 0], dict(c5, MF_EXPANDED_N="80")),
+    ]
+
+
+def main_sym9_deep():
+    """Add (or refresh) only the past-64-cell sym_fold9 chunks."""
+    path = HERE / "reference_counts.json"
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        futs = {k: ex.submit(run, cmd, env) for k, cmd, env in sym9_deep_jobs()}
+        res = {k: {"count": int(futs[k].result()), "env": env, "args": [str(c) for c in cmd[1:]]}
+               for k, cmd, env in sym9_deep_jobs()}
+    out = json.loads(path.read_text())
+    out.setdefault("sym9", {}).update(res)
+    path.write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
+    print(json.dumps(res, indent=1, sort_keys=True))
 
 
 def sym9_setup():
@@ -299,6 +326,8 @@ def main():
 if __name__ == "__main__":
     if "--cost" in sys.argv:
         main_cost()
+    elif "--sym9-deep" in sys.argv:
+        main_sym9_deep()
     elif "--sym9" in sys.argv:
         main_sym9()
     elif "--high-dim" in sys.argv:
