@@ -91,3 +91,32 @@ def test_sym_fold9_cli_chunk(golden, engine, cuda):
                          text=True, env=env, check=True)
     assert res.stdout.strip() == str(v["count"])
     assert "stream_seed_cases=465883 stream_from=25 stream_to=44" in res.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("key", ["9x9_c5_d66_first100", "9x9_c5_d80_first50"])
+def test_sym_fold9_cli_past_64_cells(golden, engine, cuda, key):
+    """MF_EXPANDED_N past 64 cells (sym_fold9.cpp:1094-1099): 96-byte cases
+    streamed in emission order, counted on the 128-bit kernel."""
+    from map_folding_gb300 import build as mfbuild
+
+    v = golden["sym9"][key]
+    env = dict(os.environ)
+    env.update(v["env"])
+    res = subprocess.run([str(mfbuild.BIN / "sym_fold9"), *v["args"]], capture_output=True,
+                         text=True, env=env, check=True)
+    assert res.stdout.strip() == str(v["count"])
+
+
+@pytest.mark.gpu
+def test_past_64_cells_need_a_chunk_size(engine, cuda):
+    """A streamed plan has no total: asking for all its cases is refused."""
+    from map_folding_gb300._native import EngineError
+
+    plan = engine.SymPlan(9, 66, center_n=5)
+    try:
+        assert plan.case_bytes == 96 and plan.total_cases == 0
+        with pytest.raises(EngineError):
+            plan.solve(0, 0)
+    finally:
+        plan.close()
