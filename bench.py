@@ -42,16 +42,16 @@ UNIT = "nodes/s"
 
 
 # DRAM bytes per case of the batched kernel: read + write of the ncu capture
-# of the first 20,000 7x7 cases (2,106,880 + 1,431,552 bytes), per case.
-TRAFFIC_PER_CASE = (2_106_880 + 1_431_552) / 20_000
+# of the first 20,000 7x7 cases (2,174,208 + 1,430,784 bytes), per case.
+TRAFFIC_PER_CASE = (2_174_208 + 1_430_784) / 20_000
 
 # Issue profile of the batched kernel from the same ncu capture (first 20,000
 # 7x7 cases searched to completion, profiles/sym_batched_7x7_first20k.md):
 # warp instructions executed per reference node and active lanes per warp
 # instruction.  The bench scales the first by its own live node rate to get
 # the kernel's warp-instruction issue rate against the SMs' issue ceiling.
-ISSUE_PROFILE = {"warp_inst_per_node": 6.65e11 / 20_803_439_733, "lanes_per_inst": 12.15,
-                 "issue_active": 0.724, "alu_pipe": 0.625,
+ISSUE_PROFILE = {"warp_inst_per_node": 528_452_558_452 / 20_803_439_733, "lanes_per_inst": 13.17,
+                 "issue_active": 0.697, "alu_pipe": 0.635,
                  "source": "profiles/sym_batched_7x7_first20k.md"}
 
 
