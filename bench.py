@@ -45,14 +45,20 @@ UNIT = "nodes/s"
 # of the first 20,000 7x7 cases (2,174,208 + 1,430,784 bytes), per case.
 TRAFFIC_PER_CASE = (2_174_208 + 1_430_784) / 20_000
 
-# Issue profile of the batched kernel from the same ncu capture (first 20,000
-# 7x7 cases searched to completion, profiles/sym_batched_7x7_first20k.md):
-# warp instructions executed per reference node and active lanes per warp
-# instruction.  The bench scales the first by its own live node rate to get
-# the kernel's warp-instruction issue rate against the SMs' issue ceiling.
-ISSUE_PROFILE = {"warp_inst_per_node": 528_452_558_452 / 20_803_439_733, "lanes_per_inst": 13.17,
-                 "issue_active": 0.697, "alu_pipe": 0.635,
-                 "source": "profiles/sym_batched_7x7_first20k.md"}
+# Issue profile of the batched kernel over one whole 7x7 count (one ncu pass
+# over a full launch of this bench's workload,
+# profiles/sym_batched_7x7_full_count.md): warp instructions executed per
+# reference node (11,214,661,565,249 over 556,214,135,282 nodes), active
+# lanes per warp instruction, and the issue-active share of SMSP cycles.  The
+# bench scales the first by its own live node rate to get the kernel's
+# warp-instruction issue rate against the SMs' issue ceiling.  The ALU-pipe
+# share comes from the fuller capture of the first 20,000 cases
+# (profiles/sym_batched_7x7_first20k.md).
+ISSUE_PROFILE = {"warp_inst_per_node": 11_214_661_565_249 / 556_214_135_282,
+                 "lanes_per_inst": 168_654_826_519_677 / 11_214_661_565_249,
+                 "issue_active": 11_214_661_565_249 / 14_115_856_002_000,
+                 "alu_pipe_first20k": 0.635,
+                 "source": "profiles/sym_batched_7x7_full_count.md"}
 
 
 def work_counts() -> dict:
