@@ -213,14 +213,126 @@ def time_cpu(cases, mults, threads, target_s=12.0):
         count = min(len(cases), int(count * max(2.0, target_s / max(el, 1e-3))))
 
 
+REF_SRC = ROOT / "baseline" / "_ref" / "src" / "sym_fold.cpp"
+REF_BIN = ROOT / "baseline" / "_ref" / "bin" / "sym_fold"
+
+
+def _ref_env():
+    """The environment for the reference binary: none of its MF_* switches
+    (case sorting, streaming, expansion depth) leak in from the caller."""
+    return {k: v for k, v in os.environ.items() if not k.startswith("MF_")}
+
+
+def _ref_runs(binary) -> bool:
+    try:
+        res = subprocess.run([str(binary), "7", "1"], capture_output=True, text=True,
+                             timeout=120, env={**_ref_env(), "MF_SETUP_ONLY": "1"})
+    except (OSError, subprocess.SubprocessError):
+        return False
+    return res.returncode == 0 and res.stdout.strip().splitlines()[-1:] == ["433131"]
+
+
+def reference_sym_fold():
+    """The reference's own CPU solver: sym_fold.cpp, staged unmodified into
+    baseline/_ref/src by oracle/Makefile (the GPU host has no reference
+    checkout), built with g++ -O3 -std=c++20 -pthread for this host, as the
+    reference's README builds it.  Returns (path, None) or (None, why)."""
+    if not REF_SRC.exists():
+        return None, ("baseline/_ref/src/sym_fold.cpp is not staged "
+                      "(make -C oracle cpu_src needs the reference checkout)")
+    if REF_BIN.exists() and REF_BIN.stat().st_mtime >= REF_SRC.stat().st_mtime \
+            and _ref_runs(REF_BIN):
+        return REF_BIN, None
+    cxx = os.environ.get("CXX") or "g++"
+    REF_BIN.parent.mkdir(parents=True, exist_ok=True)
+    tmp = REF_BIN.with_suffix(".tmp")
+    try:
+        res = subprocess.run([cxx, "-O3", "-std=c++20", "-pthread", "-o", str(tmp), str(REF_SRC)],
+                             capture_output=True, text=True, timeout=600)
+    except (OSError, subprocess.SubprocessError) as e:
+        return None, f"building sym_fold.cpp failed: {e}"
+    if res.returncode != 0:
+        return None, "building sym_fold.cpp failed: " + (res.stderr.strip().splitlines() or ["?"])[-1]
+    tmp.replace(REF_BIN)
+    if not _ref_runs(REF_BIN):
+        return None, "the built sym_fold did not list the 433131 7x7 cases"
+    return REF_BIN, None
+
+
+def reference_sample() -> dict:
+    """The reference arm's bounded sample: chunks of consecutive 7x7 cases
+    with their answers and reference nodes, counted by the oracle
+    (tests/golden/make_work_counts.py --ref-sample)."""
+    p = ROOT / "tests" / "golden" / "work_counts.json"
+    return json.loads(p.read_text()).get("7x7_d24_ref_sample", {}) if p.exists() else {}
+
+
+def time_reference_sample(binary, sample, threads):
+    """One pass of the reference binary over the sample, one
+    `sym_fold 7 <threads> <max_cases> <start_case>` process per chunk, each
+    chunk's answer checked; returns (seconds, nodes)."""
+    el_total = 0.0
+    for c in sample["chunks"]:
+        t0 = time.perf_counter()
+        res = subprocess.run([str(binary), "7", str(threads), str(c["max_cases"]),
+                              str(c["start_case"])], capture_output=True, text=True,
+                             timeout=1800, env=_ref_env())
+        el_total += time.perf_counter() - t0
+        got = res.stdout.strip().splitlines()[-1:] if res.returncode == 0 else []
+        if got != [str(c["answer"])]:
+            raise RuntimeError(f"sym_fold chunk at {c['start_case']}: rc={res.returncode} "
+                               f"stdout={got} want {c['answer']}")
+    return el_total, sample["nodes"]
+
+
+def reference_sample_desc(sample) -> str:
+    starts = ", ".join(str(c["start_case"]) for c in sample["chunks"])
+    return (f"reference sym_fold.cpp (unmodified, g++ -O3) on {len(sample['chunks'])} chunks of "
+            f"{sample['chunks'][0]['max_cases']} consecutive 7x7 depth-24 cases at starts {starts} "
+            f"of 433131, one process per chunk (its case expansion, ~0.1 s, included)")
+
+
 def run_reference(args):
-    """The reference's CPU solver (oracle restatement of sym_fold.cpp: the
-    reference's binaries cannot be built on this host) on all host threads,
-    a bounded sample per step."""
+    """The reference's own CPU solver (sym_fold.cpp built from the staged
+    source, reference_sym_fold) on all host threads, a bounded sample of the
+    7x7 count per step (reference_sample); if it cannot be built or run here,
+    the oracle's restatement of it on a strided sample, saying why."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     threads = os.cpu_count() or 1
+    binary, why = reference_sym_fold()
+    sample = reference_sample()
+    if binary is not None and not sample:
+        binary, why = None, "tests/golden/work_counts.json has no 7x7_d24_ref_sample"
+    if binary is not None:
+        try:
+            for _ in range(args.warmup):
+                time_reference_sample(binary, sample, threads)
+            times = []
+            nodes = 0
+            for _ in range(args.steps):
+                el, nodes = time_reference_sample(binary, sample, threads)
+                times.append(el)
+        except (RuntimeError, OSError, subprocess.SubprocessError) as e:
+            binary, why = None, f"running sym_fold failed: {e}"
+    if binary is not None:
+        value = nodes * len(times) / sum(times)
+        desc = reference_sample_desc(sample)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic: the reference's own 7x7 case list (deterministic)",
+            "config": {"workload": f"7x7 sym_fold depth-24 cases, CPU sample ({desc})",
+                       "n": N, "expanded_n": EXPANDED_N, "threads": threads},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "reference",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+        return
     cases, mults = all_cases_7x7()
     rate, sample, el, count = time_cpu(cases, mults, threads, target_s=8.0)
     from oracle import oracle
@@ -247,6 +359,7 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_unavailable": why,
     }
     print(json.dumps(line), flush=True)
 
@@ -360,8 +473,19 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        rate, sample, el, count = time_cpu(cycles, mults, threads, target_s=10.0)
-        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+        binary, why = reference_sym_fold()
+        ref_sample = reference_sample()
+        if binary is not None and ref_sample:
+            try:
+                el, nodes = time_reference_sample(binary, ref_sample, threads)
+                cpu = {"value": nodes / el, "unit": UNIT, "cores": threads, "kind": "reference",
+                       "sample": reference_sample_desc(ref_sample)}
+            except (RuntimeError, OSError, subprocess.SubprocessError) as e:
+                why = f"running sym_fold failed: {e}"
+        if cpu is None:
+            rate, sample, el, count = time_cpu(cycles, mults, threads, target_s=10.0)
+            cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                   "reference_unavailable": why or "no reference sample"}
 
     if rank == 0:
         line = {
